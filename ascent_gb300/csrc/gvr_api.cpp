@@ -1,0 +1,658 @@
+// gvr_api.cpp — host side of the C ABI declared in include/gvr.h.
+//
+// This is the part of vtkh::VolumeRenderer / vtkh::Renderer / Ascent's
+// rendering filters that runs on the host (opacity correction, sample
+// distance, transfer-function sampling, cameras, visibility order, domain
+// bookkeeping) plus the orchestration of the device kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gvr_internal.h"
+
+namespace {
+thread_local std::string g_last_error;
+constexpr double kPi = 3.14159265358979323846;
+}  // namespace
+
+namespace gvr {
+
+int set_error(int code, const std::string &msg)
+{
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char *what)
+{
+  const int code = e == cudaErrorMemoryAllocation ? GVR_ERR_OUT_OF_MEMORY : GVR_ERR_CUDA;
+  return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+struct V3 {
+  double x, y, z;
+};
+V3 v3(const float *p) { return {p[0], p[1], p[2]}; }
+V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+V3 operator*(V3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+V3 unit(V3 a)
+{
+  const double m = std::sqrt(dot(a, a));
+  return m > 0 ? a * (1.0 / m) : a;
+}
+V3 rotate(V3 v, V3 k, double deg)
+{
+  const double th = deg * kPi / 180.0, c = std::cos(th), s = std::sin(th);
+  return v * c + cross(k, v) * s + k * (dot(k, v) * (1 - c));
+}
+
+bool finite3(const float *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+int check_camera(const gvr_camera *c)
+{
+  if (!c) return set_error(GVR_ERR_INVALID_ARGUMENT, "camera is NULL");
+  if (!finite3(c->position) || !finite3(c->look_at) || !finite3(c->up))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "camera has non-finite vectors");
+  V3 d = v3(c->look_at) - v3(c->position);
+  if (dot(d, d) == 0) return set_error(GVR_ERR_INVALID_ARGUMENT, "camera position equals look_at");
+  if (!(c->fov_y > 0 && c->fov_y < 180))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "camera fov_y must be in (0, 180)");
+  V3 r = cross(d, v3(c->up));
+  if (dot(r, r) == 0) return set_error(GVR_ERR_INVALID_ARGUMENT, "camera up is parallel to the view direction");
+  return GVR_OK;
+}
+
+double piecewise(int n, const double *pos, const double *val, int stride, int c, double x,
+                 double dflt)
+{
+  if (n <= 0) return dflt;
+  if (x <= pos[0]) return val[c];
+  if (x >= pos[n - 1]) return val[(size_t)(n - 1) * stride + c];
+  const double *it = std::upper_bound(pos, pos + n, x);
+  const int hi = (int)(it - pos), lo = hi - 1;
+  const double w = (x - pos[lo]) / (pos[hi] - pos[lo]);
+  return val[(size_t)lo * stride + c] * (1 - w) + val[(size_t)hi * stride + c] * w;
+}
+
+}  // namespace
+
+// Per-view constants of the pinhole model the reference's partials_to_canvas
+// inverts (VolumeRenderer.cpp:303-335): look, ru = look x up, rv = ru x look,
+// per-pixel steps 2 tan(fov/2) / size divided by zoom; fov_x is derived from
+// fov_y through the aspect ratio when the image is not square.
+void make_view(const gvr_camera &cam, int width, int height, ViewDev *v)
+{
+  const V3 origin = v3(cam.position);
+  const V3 look = unit(v3(cam.look_at) - origin);
+  const V3 ru = unit(cross(look, v3(cam.up)));
+  const V3 rv = unit(cross(ru, look));
+  const float fov_y = cam.fov_y;
+  float fov_x = fov_y;
+  if (width != height) {
+    const float fovy_rad = fov_y * (float)(kPi / 180.0);
+    const float vd = std::tan(0.5f * fovy_rad);
+    const float hd = ((float)width / (float)height) * vd;
+    fov_x = 2.0f * std::atan(hd) / (float)(kPi / 180.0);
+  }
+  const float thx = std::tan((fov_x * (float)(kPi / 180.0)) * 0.5f);
+  const float thy = std::tan((fov_y * (float)(kPi / 180.0)) * 0.5f);
+  float dxs = 2 * thx / (float)width, dys = 2 * thy / (float)height;
+  if (cam.zoom > 0) {
+    dxs /= cam.zoom;
+    dys /= cam.zoom;
+  }
+  const double o[3] = {origin.x, origin.y, origin.z};
+  const double l[3] = {look.x, look.y, look.z};
+  const double r[3] = {ru.x, ru.y, ru.z};
+  const double u[3] = {rv.x, rv.y, rv.z};
+  for (int a = 0; a < 3; ++a) {
+    v->origin[a] = (float)o[a];
+    v->look[a] = (float)l[a];
+    v->ru[a] = (float)r[a];
+    v->rv[a] = (float)u[a];
+  }
+  v->dx_scale = dxs;
+  v->dy_scale = dys;
+  v->xoff = cam.xpan * (float)width * 0.5f;
+  v->yoff = cam.ypan * (float)height * 0.5f;
+  // projection * view (standard perspective look-at camera)
+  const V3 f = look;
+  const V3 s = unit(cross(f, v3(cam.up)));
+  const V3 uu = cross(s, f);
+  const double V[4][4] = {{s.x, s.y, s.z, -dot(s, origin)},
+                          {uu.x, uu.y, uu.z, -dot(uu, origin)},
+                          {-f.x, -f.y, -f.z, dot(f, origin)},
+                          {0, 0, 0, 1}};
+  const double n = cam.near_plane, fa = cam.far_plane;
+  const double aspect = (double)width / (double)height;
+  const double ff = 1.0 / std::tan(0.5 * (double)cam.fov_y * kPi / 180.0);
+  const double z = cam.zoom > 0 ? (double)cam.zoom : 1.0;
+  const double P[4][4] = {{ff / aspect * z, 0, 0, 0},
+                          {0, ff * z, 0, 0},
+                          {0, 0, (fa + n) / (n - fa), 2 * fa * n / (n - fa)},
+                          {0, 0, -1, 0}};
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double acc = 0;
+      for (int k = 0; k < 4; ++k) acc += P[i][k] * V[k][j];
+      v->projview[i * 4 + j] = (float)acc;
+    }
+}
+
+}  // namespace gvr
+
+using namespace gvr;
+
+extern "C" {
+
+const char *gvr_last_error(void) { return g_last_error.c_str(); }
+
+int gvr_version(void) { return GVR_VERSION; }
+
+int gvr_correct_opacity(const double *alpha_in, int n, int num_samples, double *alpha_out)
+{
+  if (num_samples < 1)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "Volume rendering samples must be greater than 0");
+  if (n < 0 || (n > 0 && (!alpha_in || !alpha_out)))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad alpha arrays");
+  const float ratio = 10.f / (float)num_samples;
+  for (int i = 0; i < n; ++i) alpha_out[i] = 1. - std::pow(1. - alpha_in[i], (double)ratio);
+  return GVR_OK;
+}
+
+int gvr_sample_distance(const double bounds[6], int num_samples, float *sample_dist)
+{
+  if (!bounds || !sample_dist) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (num_samples < 1)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "Volume rendering samples must be greater than 0");
+  const float e[3] = {(float)(bounds[1] - bounds[0]), (float)(bounds[3] - bounds[2]),
+                      (float)(bounds[5] - bounds[4])};
+  const float mag = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+  *sample_dist = mag / (float)num_samples;
+  return GVR_OK;
+}
+
+int gvr_color_table_sample(const gvr_color_table *t, int n, int uint8_mode, float *out)
+{
+  if (!t || !out || n < 2) return set_error(GVR_ERR_INVALID_ARGUMENT, "bad colour table arguments");
+  if (uint8_mode < GVR_UINT8_NONE || uint8_mode > GVR_UINT8_TRUNCATE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad uint8 mode");
+  for (int i = 1; i < t->n_rgb; ++i)
+    if (!(t->rgb_pos[i] > t->rgb_pos[i - 1]))
+      return set_error(GVR_ERR_INVALID_ARGUMENT, "rgb control points must be strictly increasing");
+  for (int i = 1; i < t->n_alpha; ++i)
+    if (!(t->alpha_pos[i] > t->alpha_pos[i - 1]))
+      return set_error(GVR_ERR_INVALID_ARGUMENT, "alpha control points must be strictly increasing");
+  for (int i = 0; i < n; ++i) {
+    const double x = (double)i / (double)(n - 1);
+    double c[4];
+    for (int k = 0; k < 3; ++k) c[k] = piecewise(t->n_rgb, t->rgb_pos, t->rgb, 3, k, x, 0.0);
+    c[3] = piecewise(t->n_alpha, t->alpha_pos, t->alpha, 1, 0, x, 1.0);
+    for (int k = 0; k < 4; ++k) {
+      double v = std::min(1.0, std::max(0.0, c[k]));
+      if (uint8_mode == GVR_UINT8_NONE) {
+        out[i * 4 + k] = (float)c[k];
+      } else {
+        const double s = v * 255.0;
+        unsigned u = uint8_mode == GVR_UINT8_TRUNCATE ? (unsigned)s : (unsigned)(s + 0.5);
+        out[i * 4 + k] = (float)std::min(u, 255u) * (1.0f / 255.0f);
+      }
+    }
+  }
+  return GVR_OK;
+}
+
+int gvr_camera_reset_to_bounds(gvr_camera *c, const double b[6])
+{
+  if (!c || !b) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  const double cx = 0.5 * (b[0] + b[1]), cy = 0.5 * (b[2] + b[3]), cz = 0.5 * (b[4] + b[5]);
+  const double ex = b[1] - b[0], ey = b[3] - b[2], ez = b[5] - b[4];
+  double diag = std::sqrt(ex * ex + ey * ey + ez * ez);
+  if (!(diag > 0)) diag = 1.0;
+  const double fov = 30.0;
+  const double dist = 0.5 * diag / std::tan(0.5 * fov * kPi / 180.0);
+  c->look_at[0] = (float)cx; c->look_at[1] = (float)cy; c->look_at[2] = (float)cz;
+  c->position[0] = (float)cx; c->position[1] = (float)cy; c->position[2] = (float)(cz + dist);
+  c->up[0] = 0.f; c->up[1] = 1.f; c->up[2] = 0.f;
+  c->fov_y = (float)fov;
+  c->zoom = 1.f;
+  c->xpan = 0.f;
+  c->ypan = 0.f;
+  c->near_plane = (float)(0.01 * diag);
+  c->far_plane = (float)(100.0 * diag);
+  return GVR_OK;
+}
+
+int gvr_camera_azimuth(gvr_camera *c, double deg)
+{
+  if (!c) return set_error(GVR_ERR_INVALID_ARGUMENT, "camera is NULL");
+  const V3 k = unit(v3(c->up));
+  const V3 at = v3(c->look_at);
+  const V3 p = at + rotate(v3(c->position) - at, k, deg);
+  c->position[0] = (float)p.x; c->position[1] = (float)p.y; c->position[2] = (float)p.z;
+  return GVR_OK;
+}
+
+int gvr_camera_elevation(gvr_camera *c, double deg)
+{
+  if (!c) return set_error(GVR_ERR_INVALID_ARGUMENT, "camera is NULL");
+  const V3 at = v3(c->look_at);
+  const V3 off = v3(c->position) - at;
+  const V3 k = unit(cross(off, v3(c->up)));
+  const V3 p = at + rotate(off, k, deg);
+  c->position[0] = (float)p.x; c->position[1] = (float)p.y; c->position[2] = (float)p.z;
+  return GVR_OK;
+}
+
+int gvr_cinema_cameras(const double b[6], const float *pt, int n, gvr_camera *out)
+{
+  if (!b || (n > 0 && (!pt || !out)) || n < 0)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad cinema arguments");
+  const float center[3] = {(float)(0.5 * (b[0] + b[1])), (float)(0.5 * (b[2] + b[3])),
+                           (float)(0.5 * (b[4] + b[5]))};
+  const float ext[3] = {(float)(b[1] - b[0]), (float)(b[3] - b[2]), (float)(b[5] - b[4])};
+  const float radius = std::sqrt(ext[0] * ext[0] + ext[1] * ext[1] + ext[2] * ext[2]) * 2.5f / 2.0f;
+  for (int a = 0; a < n; ++a) {
+    gvr_camera c;
+    gvr_camera_reset_to_bounds(&c, b);
+    const float phi = pt[2 * a] * (float)(kPi / 180.0);
+    const float th = pt[2 * a + 1] * (float)(kPi / 180.0);
+    const float cp = std::cos(phi), sp = std::sin(phi), ct = std::cos(th), st = std::sin(th);
+    // columns 1 (image of up = +y) and 2 (image of +z) of Rz(phi) Rx(theta)
+    const float up[3] = {-sp * ct, cp * ct, st};
+    const float pos[3] = {sp * st, -cp * st, ct};
+    const float um = std::sqrt(up[0] * up[0] + up[1] * up[1] + up[2] * up[2]);
+    for (int i = 0; i < 3; ++i) {
+      c.up[i] = up[i] / um;
+      c.position[i] = pos[i] * radius + center[i];
+      c.look_at[i] = center[i];
+    }
+    out[a] = c;
+  }
+  return GVR_OK;
+}
+
+int gvr_visibility_order(const gvr_camera *c, const double *bounds, int n, int *order)
+{
+  if (!c || n < 0 || (n > 0 && (!bounds || !order)))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad visibility-order arguments");
+  std::vector<float> dist(n);
+  for (int d = 0; d < n; ++d) {
+    const double *bb = bounds + 6 * d;
+    const float dx = (float)(0.5 * (bb[0] + bb[1])) - c->position[0];
+    const float dy = (float)(0.5 * (bb[2] + bb[3])) - c->position[1];
+    const float dz = (float)(0.5 * (bb[4] + bb[5])) - c->position[2];
+    dist[d] = std::sqrt(dx * dx + dy * dy + dz * dz);
+  }
+  std::vector<int> idx(n);
+  for (int d = 0; d < n; ++d) idx[d] = d;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b2) { return dist[a] < dist[b2]; });
+  for (int r = 0; r < n; ++r) order[idx[r]] = r;
+  return GVR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Scene
+// ---------------------------------------------------------------------------
+
+int gvr_scene_create(int device, gvr_scene **out)
+{
+  if (!out) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene_out is NULL");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceCount");
+  if (device < 0 || device >= count)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "device " + std::to_string(device) + " does not exist");
+  gvr_scene *s = new gvr_scene();
+  s->device = device;
+  *out = s;
+  return GVR_OK;
+}
+
+static void free_domain(Domain &d)
+{
+  cudaFree(d.d_bricks);
+  cudaFree(d.d_cells);
+  for (int a = 0; a < 3; ++a) cudaFree(d.d_coord[a]);
+  cudaFree(d.d_brick_range);
+  cudaFree(d.d_brick_empty);
+  d = Domain();
+}
+
+int gvr_scene_destroy(gvr_scene *s)
+{
+  if (!s) return GVR_OK;
+  cudaSetDevice(s->device);
+  for (Domain &d : s->domains) free_domain(d);
+  cudaFree(s->d_domains);
+  cudaFree(s->d_lut);
+  cudaFree(s->d_counters);
+  cudaFree(s->d_rgba_tmp);
+  cudaFree(s->d_depth_tmp);
+  delete s;
+  return GVR_OK;
+}
+
+static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, int64_t stride,
+                        int location)
+{
+  if (!field) return set_error(GVR_ERR_INVALID_ARGUMENT, "field is NULL");
+  if (dtype != GVR_DTYPE_FLOAT32 && dtype != GVR_DTYPE_FLOAT64)
+    return set_error(GVR_ERR_UNSUPPORTED, "field dtype must be float32 or float64");
+  if (stride < 1) return set_error(GVR_ERR_INVALID_ARGUMENT, "field stride must be >= 1");
+  if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad field location");
+  cudaError_t e;
+  if (d.dev.assoc == GVR_ASSOC_VERTEX) {
+    e = launch_brick_field(field, dtype, stride, location == GVR_MEM_DEVICE, d.dev.dims,
+                           d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, 0);
+  } else {
+    e = launch_cells_field(field, dtype, stride, location == GVR_MEM_DEVICE, (int64_t)d.n_values,
+                           d.d_cells, d.range, 0);
+  }
+  if (e != cudaSuccess) return cuda_error(e, "field upload");
+  if (!(std::isfinite(d.range[0]) && std::isfinite(d.range[1])))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
+  s->table_dirty = true;
+  return GVR_OK;
+}
+
+static int add_structured(gvr_scene *s, int kind, const int dims[3], const double origin[3],
+                          const double spacing[3], const double *coords[3], const void *field,
+                          int dtype, int64_t stride, int assoc, int location, int *domain_id)
+{
+  if (!s || !dims) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if ((int)s->domains.size() >= kMaxDomains)
+    return set_error(GVR_ERR_UNSUPPORTED, "a scene holds at most 64 structured domains");
+  for (int a = 0; a < 3; ++a)
+    if (dims[a] < 2) return set_error(GVR_ERR_INVALID_ARGUMENT, "every dimension needs >= 2 nodes");
+  if (assoc != GVR_ASSOC_VERTEX && assoc != GVR_ASSOC_ELEMENT)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad field association");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  Domain d;
+  std::memset(&d.dev, 0, sizeof(d.dev));
+  d.dev.kind = kind;
+  d.dev.assoc = assoc;
+  for (int a = 0; a < 3; ++a) {
+    d.dev.dims[a] = dims[a];
+    d.dev.nbrick[a] = (dims[a] - 1 + kBrickCells - 1) / kBrickCells;
+  }
+  if (kind == GVR_DOMAIN_UNIFORM) {
+    for (int a = 0; a < 3; ++a) {
+      const float o = (float)origin[a], sp = (float)spacing[a];
+      if (!(sp > 0) || !std::isfinite(o))
+        return set_error(GVR_ERR_INVALID_ARGUMENT, "uniform spacing must be > 0 and origin finite");
+      d.dev.origin[a] = o;
+      d.dev.inv_spacing[a] = 1.0f / sp;
+      d.dev.lo[a] = o;
+      d.dev.hi[a] = (float)((double)o + (double)(dims[a] - 1) * (double)sp);
+      d.bounds[2 * a] = d.dev.lo[a];
+      d.bounds[2 * a + 1] = d.dev.hi[a];
+    }
+  } else {
+    for (int a = 0; a < 3; ++a) {
+      if (!coords[a]) return set_error(GVR_ERR_INVALID_ARGUMENT, "rectilinear coordinates are NULL");
+      std::vector<float> c(dims[a]);
+      for (int i = 0; i < dims[a]; ++i) {
+        c[i] = (float)coords[a][i];
+        if (i > 0 && !(c[i] > c[i - 1]))
+          return set_error(GVR_ERR_INVALID_ARGUMENT, "rectilinear coordinates must increase");
+      }
+      e = cudaMalloc(&d.d_coord[a], sizeof(float) * dims[a]);
+      if (e != cudaSuccess) { free_domain(d); return cuda_error(e, "cudaMalloc coords"); }
+      e = cudaMemcpy(d.d_coord[a], c.data(), sizeof(float) * dims[a], cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) { free_domain(d); return cuda_error(e, "copy coords"); }
+      d.dev.coord[a] = d.d_coord[a];
+      d.dev.lo[a] = c.front();
+      d.dev.hi[a] = c.back();
+      d.dev.origin[a] = c.front();
+      d.dev.inv_spacing[a] = 1.f;
+      d.bounds[2 * a] = c.front();
+      d.bounds[2 * a + 1] = c.back();
+    }
+  }
+  if (assoc == GVR_ASSOC_VERTEX) {
+    d.n_values = (size_t)dims[0] * dims[1] * dims[2];
+    d.n_bricks = (int64_t)d.dev.nbrick[0] * d.dev.nbrick[1] * d.dev.nbrick[2];
+    e = cudaMalloc(&d.d_bricks, sizeof(float) * kBrickFloats * d.n_bricks);
+    if (e == cudaSuccess) e = cudaMalloc(&d.d_brick_range, sizeof(float2) * d.n_bricks);
+    if (e == cudaSuccess) e = cudaMalloc(&d.d_brick_empty, d.n_bricks);
+    if (e == cudaSuccess) e = cudaMemset(d.d_brick_empty, 0, d.n_bricks);
+  } else {
+    d.n_values = (size_t)(dims[0] - 1) * (dims[1] - 1) * (dims[2] - 1);
+    e = cudaMalloc(&d.d_cells, sizeof(float) * d.n_values);
+  }
+  if (e != cudaSuccess) { free_domain(d); return cuda_error(e, "cudaMalloc field"); }
+  d.dev.bricks = d.d_bricks;
+  d.dev.cells = d.d_cells;
+  d.dev.brick_range = d.d_brick_range;
+  d.dev.brick_empty = d.d_brick_empty;
+  int rc = upload_field(s, d, field, dtype, stride, location);
+  if (rc != GVR_OK) { free_domain(d); return rc; }
+  s->domains.push_back(d);
+  s->table_dirty = true;
+  if (domain_id) *domain_id = (int)s->domains.size() - 1;
+  return GVR_OK;
+}
+
+int gvr_scene_add_uniform(gvr_scene *s, const int dims[3], const double origin[3],
+                          const double spacing[3], const void *field, int dtype, int64_t stride,
+                          int association, int location, int *domain_id)
+{
+  if (!origin || !spacing) return set_error(GVR_ERR_INVALID_ARGUMENT, "origin/spacing is NULL");
+  const double *coords[3] = {nullptr, nullptr, nullptr};
+  return add_structured(s, GVR_DOMAIN_UNIFORM, dims, origin, spacing, coords, field, dtype, stride,
+                        association, location, domain_id);
+}
+
+int gvr_scene_add_rectilinear(gvr_scene *s, const int dims[3], const double *x, const double *y,
+                              const double *z, const void *field, int dtype, int64_t stride,
+                              int association, int location, int *domain_id)
+{
+  const double *coords[3] = {x, y, z};
+  return add_structured(s, GVR_DOMAIN_RECTILINEAR, dims, nullptr, nullptr, coords, field, dtype,
+                        stride, association, location, domain_id);
+}
+
+int gvr_scene_update_field(gvr_scene *s, int domain_id, const void *field, int dtype,
+                           int64_t stride, int location)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (domain_id < 0 || domain_id >= (int)s->domains.size())
+    return set_error(GVR_ERR_NOT_FOUND, "no such domain");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  return upload_field(s, s->domains[domain_id], field, dtype, stride, location);
+}
+
+int gvr_scene_num_domains(const gvr_scene *s, int *n)
+{
+  if (!s || !n) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = (int)s->domains.size();
+  return GVR_OK;
+}
+
+int gvr_scene_bounds(const gvr_scene *s, int domain_id, double b[6])
+{
+  if (!s || !b) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (domain_id >= (int)s->domains.size() || domain_id < -1)
+    return set_error(GVR_ERR_NOT_FOUND, "no such domain");
+  if (domain_id >= 0) {
+    std::memcpy(b, s->domains[domain_id].bounds, sizeof(double) * 6);
+    return GVR_OK;
+  }
+  if (s->domains.empty()) return set_error(GVR_ERR_NOT_FOUND, "scene has no domains");
+  for (int a = 0; a < 3; ++a) {
+    b[2 * a] = INFINITY;
+    b[2 * a + 1] = -INFINITY;
+  }
+  for (const Domain &d : s->domains)
+    for (int a = 0; a < 3; ++a) {
+      b[2 * a] = std::min(b[2 * a], d.bounds[2 * a]);
+      b[2 * a + 1] = std::max(b[2 * a + 1], d.bounds[2 * a + 1]);
+    }
+  return GVR_OK;
+}
+
+int gvr_scene_range(const gvr_scene *s, double r[2])
+{
+  if (!s || !r) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (s->domains.empty()) return set_error(GVR_ERR_NOT_FOUND, "scene has no domains");
+  r[0] = INFINITY;
+  r[1] = -INFINITY;
+  for (const Domain &d : s->domains) {
+    r[0] = std::min(r[0], d.range[0]);
+    r[1] = std::max(r[1], d.range[1]);
+  }
+  return GVR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Render
+// ---------------------------------------------------------------------------
+
+static int check_params(const gvr_render_params *p)
+{
+  if (!p) return set_error(GVR_ERR_INVALID_ARGUMENT, "params is NULL");
+  if (p->width < 1 || p->height < 1 || (int64_t)p->width * p->height > (1ll << 28))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "image size must be >= 1 and <= 2^28 pixels");
+  if (!(p->sample_dist > 0) || !std::isfinite(p->sample_dist))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "sample_dist must be > 0");
+  if (!p->lut_rgba || p->lut_size < 2 || p->lut_size > kMaxLut)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "lut_size must be in [2, 4096]");
+  if (p->lut_filter != GVR_LUT_NEAREST && p->lut_filter != GVR_LUT_LINEAR)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad lut_filter");
+  if (!std::isfinite(p->scalar_min) || !std::isfinite(p->scalar_max))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "scalar range must be finite");
+  return GVR_OK;
+}
+
+static int ensure_buffers(gvr_scene *s, int64_t pixels, int lut_size)
+{
+  cudaError_t e;
+  if (s->table_dirty || s->d_domains_cap < (int)s->domains.size()) {
+    if (s->d_domains_cap < (int)s->domains.size()) {
+      cudaFree(s->d_domains);
+      s->d_domains = nullptr;
+      e = cudaMalloc(&s->d_domains, sizeof(DomainDev) * kMaxDomains);
+      if (e != cudaSuccess) return cuda_error(e, "cudaMalloc domain table");
+      s->d_domains_cap = kMaxDomains;
+    }
+    std::vector<DomainDev> h(s->domains.size());
+    for (size_t i = 0; i < h.size(); ++i) h[i] = s->domains[i].dev;
+    if (!h.empty()) {
+      e = cudaMemcpy(s->d_domains, h.data(), sizeof(DomainDev) * h.size(), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_error(e, "copy domain table");
+    }
+    s->table_dirty = false;
+  }
+  if (!s->d_lut) {
+    e = cudaMalloc(&s->d_lut, sizeof(float4) * kMaxLut);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMalloc LUT");
+  }
+  if (!s->d_counters) {
+    e = cudaMalloc(&s->d_counters, sizeof(unsigned long long) * 4);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMalloc counters");
+  }
+  if (pixels > s->tmp_pixels) {
+    cudaFree(s->d_rgba_tmp);
+    cudaFree(s->d_depth_tmp);
+    s->d_rgba_tmp = nullptr;
+    s->d_depth_tmp = nullptr;
+    s->tmp_pixels = 0;
+    e = cudaMalloc(&s->d_rgba_tmp, sizeof(float4) * pixels);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_depth_tmp, sizeof(float) * pixels);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMalloc image");
+    s->tmp_pixels = pixels;
+  }
+  (void)lut_size;
+  return GVR_OK;
+}
+
+int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
+                      float *rgba, float *depth, int out_location, void *stream,
+                      uint64_t *samples_out)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  int rc = check_camera(camera);
+  if (rc != GVR_OK) return rc;
+  if ((rc = check_params(p)) != GVR_OK) return rc;
+  if (!rgba || !depth) return set_error(GVR_ERR_INVALID_ARGUMENT, "output buffers are NULL");
+  if (out_location != GVR_MEM_HOST && out_location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad out_location");
+  if (s->domains.empty()) return set_error(GVR_ERR_NOT_FOUND, "scene has no domains");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t pixels = (int64_t)p->width * p->height;
+  if ((rc = ensure_buffers(s, out_location == GVR_MEM_HOST ? pixels : 0, p->lut_size)) != GVR_OK)
+    return rc;
+
+  MarchParams mp;
+  std::memset(&mp, 0, sizeof(mp));
+  mp.width = p->width;
+  mp.height = p->height;
+  mp.n_domains = (int)s->domains.size();
+  mp.lut_size = p->lut_size;
+  mp.lut_filter = p->lut_filter;
+  mp.quantize_uint8 = p->quantize_uint8 ? 1 : 0;
+  mp.render_bg = p->render_bg ? 1 : 0;
+  mp.sample_dist = p->sample_dist;
+  mp.scalar_min = p->scalar_min;
+  mp.inv_range = p->scalar_max > p->scalar_min ? 1.0f / (p->scalar_max - p->scalar_min) : 0.f;
+  mp.alpha_cull = p->alpha_cull;
+  mp.early_term = p->early_term >= 1.f ? 2.f : p->early_term;
+  mp.clear_depth = p->clear_depth;
+  for (int c = 0; c < 4; ++c) mp.bg[c] = p->bg_color[c];
+
+  e = cudaMemcpyAsync(s->d_lut, p->lut_rgba, sizeof(float4) * p->lut_size, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_error(e, "copy LUT");
+  // empty-space skipping: classify bricks against this transfer function
+  mp.skip_empty = 1;
+  for (Domain &d : s->domains) {
+    if (d.dev.assoc != GVR_ASSOC_VERTEX) continue;
+    e = launch_empty_bricks(d.d_brick_range, d.n_bricks, s->d_lut, p->lut_size, p->lut_filter,
+                            mp.scalar_min, mp.inv_range, d.d_brick_empty, st);
+    if (e != cudaSuccess) return cuda_error(e, "empty-brick pass");
+  }
+  if (samples_out) {
+    e = cudaMemsetAsync(s->d_counters, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return cuda_error(e, "clear counters");
+  }
+  ViewDev view;
+  make_view(*camera, p->width, p->height, &view);
+  float4 *d_rgba = out_location == GVR_MEM_DEVICE ? (float4 *)rgba : s->d_rgba_tmp;
+  float *d_depth = out_location == GVR_MEM_DEVICE ? depth : s->d_depth_tmp;
+  e = launch_march(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
+                   samples_out ? s->d_counters : nullptr, st);
+  if (e != cudaSuccess) return cuda_error(e, "march kernel launch");
+  if (out_location == GVR_MEM_HOST) {
+    e = cudaMemcpyAsync(rgba, d_rgba, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(depth, d_depth, sizeof(float) * pixels, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return cuda_error(e, "copy image to host");
+  }
+  if (samples_out) {
+    unsigned long long n = 0;
+    e = cudaMemcpyAsync(&n, s->d_counters, sizeof(n), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "read sample counter");
+    *samples_out = n;
+  } else if (out_location == GVR_MEM_HOST) {
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "render");
+  }
+  return GVR_OK;
+}
+
+}  // extern "C"

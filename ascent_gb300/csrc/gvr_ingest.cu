@@ -1,0 +1,231 @@
+// gvr_ingest.cu — field upload into the bricked device layout.
+//
+// Replaces the field half of the Blueprint -> VTK-m adapter
+// (ascent_vtkh_data_adapter.cpp:1782-2040, AddField: float32/float64,
+// strided, vertex/element) and the scalar-range pass of
+// Renderer::PreExecute (Renderer.cpp:144-179). The output layout is the
+// renderer's own: 8^3-cell bricks with a one-node apron plus a per-brick
+// {min,max} macrocell grid used for empty-space skipping.
+#include <cfloat>
+#include <cstdio>
+
+#include "gvr_internal.h"
+
+namespace gvr {
+namespace {
+
+__device__ __forceinline__ float load_value(const void *src, int dtype, int64_t i)
+{
+  return dtype == GVR_DTYPE_FLOAT64 ? (float)((const double *)src)[i]
+                                    : ((const float *)src)[i];
+}
+
+// One CTA per brick: gather the brick's 9^3 nodes (clamped at the domain's
+// last node), write them to the brick, and reduce their min/max.
+__global__ void __launch_bounds__(256)
+brick_kernel(const void *__restrict__ src, int dtype, int64_t stride, int nx,
+             int ny, int nz, int nbx, int nby, float *__restrict__ bricks,
+             float2 *__restrict__ brick_range)
+{
+  const int64_t b = blockIdx.x;
+  const int bx = (int)(b % nbx);
+  const int by = (int)((b / nbx) % nby);
+  const int bz = (int)(b / ((int64_t)nbx * nby));
+  float vmin = FLT_MAX, vmax = -FLT_MAX;
+  int bad = 0;
+  float *dst = bricks + b * kBrickFloats;
+  for (int l = threadIdx.x; l < kBrickFloats; l += blockDim.x) {
+    float v = 0.f;
+    if (l < kBrickNodes * kBrickNodes * kBrickNodes) {
+      const int lx = l % kBrickNodes;
+      const int ly = (l / kBrickNodes) % kBrickNodes;
+      const int lz = l / (kBrickNodes * kBrickNodes);
+      const int x = min(bx * kBrickCells + lx, nx - 1);
+      const int y = min(by * kBrickCells + ly, ny - 1);
+      const int z = min(bz * kBrickCells + lz, nz - 1);
+      const int64_t idx = ((int64_t)z * ny + y) * nx + x;
+      v = load_value(src, dtype, idx * stride);
+      bad |= !isfinite(v);
+      vmin = fminf(vmin, v);
+      vmax = fmaxf(vmax, v);
+    }
+    dst[l] = v;
+  }
+  bad = __syncthreads_or(bad);
+  // block min/max
+  for (int o = 16; o > 0; o >>= 1) {
+    vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  }
+  __shared__ float smin[8], smax[8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { smin[w] = vmin; smax[w] = vmax; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+      vmin = fminf(vmin, smin[i]);
+      vmax = fmaxf(vmax, smax[i]);
+    }
+    brick_range[b] = bad ? make_float2(NAN, NAN) : make_float2(vmin, vmax);
+  }
+}
+
+// Strided float32/float64 -> contiguous float32 with per-CTA min/max.
+__global__ void __launch_bounds__(256)
+convert_kernel(const void *__restrict__ src, int dtype, int64_t stride, int64_t n,
+               float *__restrict__ dst, float2 *__restrict__ block_range)
+{
+  float vmin = FLT_MAX, vmax = -FLT_MAX;
+  int bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = load_value(src, dtype, i * stride);
+    bad |= !isfinite(v);
+    dst[i] = v;
+    vmin = fminf(vmin, v);
+    vmax = fmaxf(vmax, v);
+  }
+  bad = __syncthreads_or(bad);
+  for (int o = 16; o > 0; o >>= 1) {
+    vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  }
+  __shared__ float smin[8], smax[8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { smin[w] = vmin; smax[w] = vmax; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+      vmin = fminf(vmin, smin[i]);
+      vmax = fmaxf(vmax, smax[i]);
+    }
+    block_range[blockIdx.x] = bad ? make_float2(NAN, NAN) : make_float2(vmin, vmax);
+  }
+}
+
+// A brick is empty when the transfer function's opacity is zero over every
+// LUT entry its scalar range can reach.
+__global__ void empty_kernel(const float2 *__restrict__ brick_range, int64_t n,
+                             const float4 *__restrict__ lut, int lut_size,
+                             int lut_filter, float smin, float inv_range,
+                             uint8_t *__restrict__ empty)
+{
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < n;
+       b += (int64_t)gridDim.x * blockDim.x) {
+    const float2 r = brick_range[b];
+    const float s0 = __saturatef((r.x - smin) * inv_range);
+    const float s1 = __saturatef((r.y - smin) * inv_range);
+    const float x0 = s0 * (float)(lut_size - 1);
+    const float x1 = s1 * (float)(lut_size - 1);
+    int i0 = (int)x0;
+    int i1 = lut_filter == GVR_LUT_LINEAR ? (int)ceilf(x1) : (int)x1;
+    i0 = max(0, min(i0, lut_size - 1));
+    i1 = max(0, min(i1, lut_size - 1));
+    uint8_t e = 1;
+    for (int i = i0; i <= i1; ++i)
+      if (lut[i].w > 0.f) { e = 0; break; }
+    empty[b] = e;
+  }
+}
+
+cudaError_t stage_source(const void *src, int dtype, int64_t stride,
+                         int src_on_device, int64_t n, const void **dsrc,
+                         void **owned, cudaStream_t stream)
+{
+  *owned = nullptr;
+  if (src_on_device) {
+    *dsrc = src;
+    return cudaSuccess;
+  }
+  const size_t esz = dtype == GVR_DTYPE_FLOAT64 ? 8 : 4;
+  const size_t bytes = (size_t)((n - 1) * stride + 1) * esz;
+  cudaError_t e = cudaMalloc(owned, bytes);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(*owned, src, bytes, cudaMemcpyHostToDevice, stream);
+  *dsrc = *owned;
+  return e;
+}
+
+}  // namespace
+
+cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
+                               int src_on_device, const int dims[3],
+                               float *d_bricks, const int nbrick[3],
+                               float2 *d_brick_range, double range_out[2],
+                               cudaStream_t stream)
+{
+  const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
+  const void *dsrc = nullptr;
+  void *owned = nullptr;
+  cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, &owned, stream);
+  if (e != cudaSuccess) return e;
+  const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
+  brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1],
+                                                 dims[2], nbrick[0], nbrick[1], d_bricks,
+                                                 d_brick_range);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  std::vector<float2> h((size_t)nb);
+  e = cudaMemcpyAsync(h.data(), d_brick_range, sizeof(float2) * nb,
+                      cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (owned) cudaFree(owned);
+  if (e != cudaSuccess) return e;
+  double lo = INFINITY, hi = -INFINITY;
+  for (const float2 &r : h) {
+    if (r.x != r.x || r.y != r.y) { lo = NAN; hi = NAN; break; }
+    lo = r.x < lo ? r.x : lo;
+    hi = r.y > hi ? r.y : hi;
+  }
+  range_out[0] = lo;
+  range_out[1] = hi;
+  return cudaSuccess;
+}
+
+cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
+                               int src_on_device, int64_t n, float *d_cells,
+                               double range_out[2], cudaStream_t stream)
+{
+  const void *dsrc = nullptr;
+  void *owned = nullptr;
+  cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, &owned, stream);
+  if (e != cudaSuccess) return e;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  float2 *d_br = nullptr;
+  e = cudaMalloc(&d_br, sizeof(float2) * blocks);
+  if (e != cudaSuccess) { if (owned) cudaFree(owned); return e; }
+  convert_kernel<<<blocks, 256, 0, stream>>>(dsrc, dtype, stride, n, d_cells, d_br);
+  e = cudaGetLastError();
+  std::vector<float2> h(blocks);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h.data(), d_br, sizeof(float2) * blocks, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  cudaFree(d_br);
+  if (owned) cudaFree(owned);
+  if (e != cudaSuccess) return e;
+  double lo = INFINITY, hi = -INFINITY;
+  for (const float2 &r : h) {
+    if (r.x != r.x || r.y != r.y) { lo = NAN; hi = NAN; break; }
+    lo = r.x < lo ? r.x : lo;
+    hi = r.y > hi ? r.y : hi;
+  }
+  range_out[0] = lo;
+  range_out[1] = hi;
+  return cudaSuccess;
+}
+
+cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
+                                const float4 *d_lut, int lut_size, int lut_filter,
+                                float scalar_min, float inv_range,
+                                uint8_t *brick_empty, cudaStream_t stream)
+{
+  if (n_bricks == 0) return cudaSuccess;
+  int blocks = (int)((n_bricks + 255) / 256);
+  if (blocks > 1216) blocks = 1216;
+  empty_kernel<<<blocks, 256, 0, stream>>>(brick_range, n_bricks, d_lut, lut_size,
+                                           lut_filter, scalar_min, inv_range, brick_empty);
+  return cudaGetLastError();
+}
+
+}  // namespace gvr

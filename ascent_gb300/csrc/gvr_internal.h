@@ -1,0 +1,133 @@
+// gvr_internal.h — types shared by the host library and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gvr.h"
+
+namespace gvr {
+
+// Bricked field layout: a brick covers 8^3 cells and stores the 9^3 nodes
+// that bound them (one-node apron shared with the next brick), so every
+// cell's eight corners sit in one brick at fixed offsets. Bricks are padded
+// to 736 floats (2944 B, 23 x 128 B lines) so that each starts on a
+// 128-byte boundary.
+constexpr int kBrickCells = 8;
+constexpr int kBrickNodes = kBrickCells + 1;
+constexpr int kBrickFloats = 736;
+static_assert(kBrickNodes * kBrickNodes * kBrickNodes <= kBrickFloats, "brick");
+
+constexpr int kMaxDomains = 64;     // domains a single render can composite
+constexpr int kMaxLut = 4096;
+
+// Device view of one structured domain.
+struct DomainDev {
+  float lo[3];            // bounds
+  float hi[3];
+  float origin[3];        // uniform: node 0 position
+  float inv_spacing[3];   // uniform: 1 / spacing
+  int dims[3];            // node counts
+  int nbrick[3];          // bricks per axis
+  int kind;               // GVR_DOMAIN_UNIFORM / RECTILINEAR
+  int assoc;              // GVR_ASSOC_VERTEX / ELEMENT
+  const float *bricks;    // vertex fields: bricked nodes
+  const float *cells;     // element fields: linear cell values
+  const float *coord[3];  // rectilinear node coordinates
+  const float2 *brick_range;  // per-brick {min, max} of the field
+  const uint8_t *brick_empty; // per-brick 1 = LUT alpha is 0 over its range
+};
+
+// Everything the march kernel needs for one view.
+struct ViewDev {
+  float origin[3];        // camera position
+  float look[3];          // unit view direction
+  float ru[3];            // unit right
+  float rv[3];            // unit up (orthogonalised)
+  float dx_scale;         // world step per pixel along ru
+  float dy_scale;         // world step per pixel along rv
+  float xoff;             // pan, in pixels
+  float yoff;
+  float projview[16];     // row-major projection * view (image depth)
+};
+
+struct MarchParams {
+  int width;
+  int height;
+  int n_domains;
+  int lut_size;
+  int lut_filter;
+  int quantize_uint8;
+  int render_bg;
+  int skip_empty;
+  float sample_dist;
+  float scalar_min;
+  float inv_range;
+  float alpha_cull;
+  float early_term;
+  float clear_depth;
+  float bg[4];
+};
+
+// Host-side record of a domain owned by a scene.
+struct Domain {
+  DomainDev dev;
+  double bounds[6];
+  double range[2];
+  size_t n_values = 0;             // field values
+  float *d_bricks = nullptr;
+  float *d_cells = nullptr;
+  float *d_coord[3] = {nullptr, nullptr, nullptr};
+  float2 *d_brick_range = nullptr;
+  uint8_t *d_brick_empty = nullptr;
+  int64_t n_bricks = 0;
+};
+
+}  // namespace gvr
+
+struct gvr_scene {
+  int device = 0;
+  std::vector<gvr::Domain> domains;
+  gvr::DomainDev *d_domains = nullptr;   // device copy of the domain table
+  int d_domains_cap = 0;
+  float4 *d_lut = nullptr;               // LUT of the last render
+  unsigned long long *d_counters = nullptr;  // [0] samples
+  float4 *d_rgba_tmp = nullptr;          // device image for host outputs
+  float *d_depth_tmp = nullptr;
+  int64_t tmp_pixels = 0;
+  bool table_dirty = true;
+};
+
+namespace gvr {
+
+// error plumbing (gvr_api.cpp)
+int set_error(int code, const std::string &msg);
+int cuda_error(cudaError_t e, const char *what);
+
+// camera -> per-view constants (gvr_api.cpp)
+void make_view(const gvr_camera &cam, int width, int height, ViewDev *v);
+
+// ingest kernels (gvr_ingest.cu)
+cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
+                               int src_on_device, const int dims[3],
+                               float *d_bricks, const int nbrick[3],
+                               float2 *d_brick_range, double range_out[2],
+                               cudaStream_t stream);
+cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
+                               int src_on_device, int64_t n, float *d_cells,
+                               double range_out[2], cudaStream_t stream);
+cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
+                                const float4 *d_lut, int lut_size, int lut_filter,
+                                float scalar_min, float inv_range,
+                                uint8_t *brick_empty, cudaStream_t stream);
+
+// march kernel (gvr_march.cu)
+cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
+                         const MarchParams &mp, const float4 *d_lut,
+                         float4 *d_rgba, float *d_depth,
+                         unsigned long long *d_samples, cudaStream_t stream);
+
+}  // namespace gvr

@@ -1,0 +1,348 @@
+// gvr_march.cu — fused structured ray march + partial compositing.
+//
+// One thread per ray; a warp marches an 8x4-pixel packet and a CTA a 16x16
+// tile, so neighbouring lanes read neighbouring bricks. For every pixel the
+// kernel does what the reference spreads over several host passes:
+//   - per-domain ray setup and march        (StructuredWrapper::render,
+//     VolumeRenderer.cpp:223-284; the march itself is VTK-m's
+//     VolumeRendererStructured),
+//   - partial extraction with the alpha < alpha_cull drop and depth = the
+//     ray's exit distance of the domain    (VolumeRenderer.cpp:262-283),
+//   - compositing of the partials of all domains in increasing depth with
+//     VolumePartial::blend                  (PartialCompositor.cpp:57-90,
+//     331-490; VolumePartial.hpp:86-95),
+//   - partials_to_canvas: blend over the cleared canvas and image depth
+//     0.5 z/w + 0.49                        (VolumeRenderer.cpp:287-391),
+//   - the uint8 round trip of the single-domain path (Image.hpp:102-105,
+//     Renderer.cpp:265-283) and the background blend.
+// Domains are visited in increasing exit distance along each ray, which is
+// the order the reference's (pixel, depth) sort produces, so no partial
+// buffer or sort pass is needed.
+#include <cfloat>
+
+#include "gvr_internal.h"
+
+namespace gvr {
+namespace {
+
+constexpr int kTile = 16;     // CTA tile edge in pixels
+constexpr int kThreads = 256; // 8 warps, each an 8x4 packet
+
+struct Ray {
+  float o[3];
+  float d[3];
+};
+
+__device__ __forceinline__ bool slab(const DomainDev &dm, const Ray &r, float &t0,
+                                     float &t1)
+{
+  float tmin = 0.f, tmax = FLT_MAX;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (r.d[a] != 0.f) {
+      const float inv = 1.f / r.d[a];
+      float ta = (dm.lo[a] - r.o[a]) * inv;
+      float tb = (dm.hi[a] - r.o[a]) * inv;
+      if (ta > tb) { const float t = ta; ta = tb; tb = t; }
+      tmin = fmaxf(tmin, ta);
+      tmax = fminf(tmax, tb);
+    } else if (r.o[a] < dm.lo[a] || r.o[a] > dm.hi[a]) {
+      return false;
+    }
+  }
+  t0 = tmin;
+  t1 = tmax;
+  return tmax > tmin;
+}
+
+__device__ __forceinline__ float lerpf(float a, float b, float w)
+{
+  return fmaf(w, b - a, a);
+}
+
+__device__ __forceinline__ float4 lut_fetch(const float4 *lut, int n, int filter, float s)
+{
+  if (filter == GVR_LUT_LINEAR) {
+    const float x = s * (float)(n - 1);
+    int i0 = min((int)x, n - 2);
+    const float w = x - (float)i0;
+    const float4 a = lut[i0], b = lut[i0 + 1];
+    return make_float4(lerpf(a.x, b.x, w), lerpf(a.y, b.y, w), lerpf(a.z, b.z, w),
+                       lerpf(a.w, b.w, w));
+  }
+  const int i = min((int)(s * (float)(n - 1)), n - 1);
+  return lut[i];
+}
+
+// Rectilinear axis search: move the cell index until x[i] <= p <= x[i+1].
+__device__ __forceinline__ int rect_cell(const float *__restrict__ x, int n, float p, int i)
+{
+  while (i < n - 2 && p > __ldg(x + i + 1)) ++i;
+  while (i > 0 && p < __ldg(x + i)) --i;
+  return i;
+}
+
+// March one structured domain over [t0, t1): accumulates the domain's
+// partial in acc and returns the number of samples the stepping rule takes.
+__device__ int march_domain(const DomainDev &dm, const Ray &r, float t0, float t1,
+                            const MarchParams &mp, const float4 *lut, float thr,
+                            float4 &acc)
+{
+  const float dt = mp.sample_dist;
+  int count = 0;
+  const int nx = dm.dims[0], ny = dm.dims[1], nz = dm.dims[2];
+  const float gmax[3] = {(float)(nx - 1), (float)(ny - 1), (float)(nz - 1)};
+  // grid coordinates g = A + t B (uniform)
+  float A[3], B[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    A[a] = (r.o[a] - dm.origin[a]) * dm.inv_spacing[a];
+    B[a] = r.d[a] * dm.inv_spacing[a];
+  }
+  int rc[3] = {0, 0, 0};  // rectilinear cell indices carried along the ray
+  if (dm.kind == GVR_DOMAIN_RECTILINEAR) {
+    // first-sample binary search per axis
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float p = fmaf(t0, r.d[a], r.o[a]);
+      int lo = 0, hi = dm.dims[a] - 1;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(dm.coord[a] + mid) <= p) lo = mid; else hi = mid;
+      }
+      rc[a] = min(lo, dm.dims[a] - 2);
+    }
+  }
+  const int nbx = dm.nbrick[0], nby = dm.nbrick[1];
+  const float inv_dt = 1.f / dt;
+  for (int k = 0;; ++k) {
+    const float t = fmaf((float)k, dt, t0);
+    if (!(t < t1)) break;
+    ++count;
+    int c[3];
+    float w[3];
+    if (dm.kind == GVR_DOMAIN_UNIFORM) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float g = fminf(fmaxf(fmaf(t, B[a], A[a]), 0.f), gmax[a]);
+        c[a] = min((int)g, dm.dims[a] - 2);
+        w[a] = g - (float)c[a];
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float p = fmaf(t, r.d[a], r.o[a]);
+        rc[a] = rect_cell(dm.coord[a], dm.dims[a], p, rc[a]);
+        const float x0 = __ldg(dm.coord[a] + rc[a]);
+        const float x1 = __ldg(dm.coord[a] + rc[a] + 1);
+        c[a] = rc[a];
+        w[a] = __saturatef((p - x0) / (x1 - x0));
+      }
+    }
+    float v;
+    if (dm.assoc == GVR_ASSOC_ELEMENT) {
+      v = __ldg(dm.cells + ((int64_t)c[2] * (ny - 1) + c[1]) * (nx - 1) + c[0]);
+    } else {
+      const int bx = c[0] >> 3, by = c[1] >> 3, bz = c[2] >> 3;
+      const int64_t brick = ((int64_t)bz * nby + by) * nbx + bx;
+      if (mp.skip_empty && dm.brick_empty[brick]) {
+        // Empty brick: every sample inside it has zero opacity. Jump to the
+        // last sample before the brick's exit; those samples still count.
+        float texit = t1;
+        const int b3[3] = {bx, by, bz};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          if (dm.kind == GVR_DOMAIN_UNIFORM && B[a] != 0.f) {
+            const float edge = B[a] > 0.f ? (float)min((b3[a] + 1) * kBrickCells, dm.dims[a] - 1)
+                                          : (float)(b3[a] * kBrickCells);
+            texit = fminf(texit, (edge - A[a]) / B[a]);
+          }
+        }
+        if (dm.kind == GVR_DOMAIN_UNIFORM) {
+          const int knew = (int)floorf((texit - t0) * inv_dt);
+          if (knew > k + 1) {
+            // samples k+1 .. knew-1 are skipped; they satisfy t < texit <= t1
+            int skipped = knew - 1 - k;
+            count += skipped;
+            k = knew - 1;
+          }
+        }
+        continue;
+      }
+      const float *p = dm.bricks + brick * kBrickFloats +
+                       ((c[2] & 7) * kBrickNodes + (c[1] & 7)) * kBrickNodes + (c[0] & 7);
+      const float v000 = __ldg(p), v100 = __ldg(p + 1);
+      const float v010 = __ldg(p + kBrickNodes), v110 = __ldg(p + kBrickNodes + 1);
+      const float v001 = __ldg(p + kBrickNodes * kBrickNodes);
+      const float v101 = __ldg(p + kBrickNodes * kBrickNodes + 1);
+      const float v011 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
+      const float v111 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+      const float c00 = lerpf(v000, v100, w[0]);
+      const float c10 = lerpf(v010, v110, w[0]);
+      const float c01 = lerpf(v001, v101, w[0]);
+      const float c11 = lerpf(v011, v111, w[0]);
+      const float c0 = lerpf(c00, c10, w[1]);
+      const float c1 = lerpf(c01, c11, w[1]);
+      v = lerpf(c0, c1, w[2]);
+    }
+    const float s = __saturatef((v - mp.scalar_min) * mp.inv_range);
+    const float4 col = lut_fetch(lut, mp.lut_size, mp.lut_filter, s);
+    const float wa = (1.f - acc.w) * col.w;
+    acc.x = fmaf(wa, col.x, acc.x);
+    acc.y = fmaf(wa, col.y, acc.y);
+    acc.z = fmaf(wa, col.z, acc.z);
+    acc.w += wa;
+    if (acc.w >= thr) break;
+  }
+  return count;
+}
+
+__global__ void __launch_bounds__(kThreads)
+march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
+             const MarchParams mp, const float4 *__restrict__ g_lut,
+             float4 *__restrict__ rgba, float *__restrict__ depth,
+             unsigned long long *__restrict__ samples)
+{
+  extern __shared__ float4 smem[];
+  float4 *lut = smem;
+  DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
+  for (int i = threadIdx.x; i < mp.lut_size; i += kThreads) lut[i] = g_lut[i];
+  {
+    const int words = mp.n_domains * (int)(sizeof(DomainDev) / 4);
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(g_domains);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(doms);
+    for (int i = threadIdx.x; i < words; i += kThreads) dst[i] = src[i];
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int px = blockIdx.x * kTile + (warp & 1) * 8 + (lane & 7);
+  const int py = blockIdx.y * kTile + (warp >> 1) * 4 + (lane >> 3);
+  const bool valid = px < mp.width && py < mp.height;
+
+  int count = 0;
+  if (valid) {
+    Ray r;
+    const float fx = view.dx_scale * ((float)px - 0.5f * (float)mp.width - view.xoff);
+    const float fy = view.dy_scale * ((float)py - 0.5f * (float)mp.height - view.yoff);
+    float d[3], dn = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      d[a] = view.look[a] + view.ru[a] * fx + view.rv[a] * fy;
+      dn = fmaf(d[a], d[a], dn);
+    }
+    const float inv = rsqrtf(dn);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      r.o[a] = view.origin[a];
+      r.d[a] = d[a] * inv;
+    }
+
+    float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f;
+    bool have = false;
+    float last_t1 = -FLT_MAX;
+    int last_d = -1;
+    for (;;) {
+      if (ca >= mp.early_term) break;
+      // next domain along the ray by (exit distance, index)
+      int best = -1;
+      float bt0 = 0.f, bt1 = FLT_MAX;
+      for (int dd = 0; dd < mp.n_domains; ++dd) {
+        float t0, t1;
+        if (!slab(doms[dd], r, t0, t1)) continue;
+        const bool after = t1 > last_t1 || (t1 == last_t1 && dd > last_d);
+        const bool before = best < 0 || t1 < bt1;
+        if (after && before) { best = dd; bt0 = t0; bt1 = t1; }
+      }
+      if (best < 0) break;
+      last_t1 = bt1;
+      last_d = best;
+      const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      count += march_domain(doms[best], r, bt0, bt1, mp, lut, thr, acc);
+      if (acc.w < mp.alpha_cull) continue;
+      if (!have) {
+        crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
+        cdepth = bt1;
+        have = true;
+      } else if (ca < 1.f && acc.w != 0.f) {
+        const float op = 1.f - ca;
+        crgb[0] = fmaf(op, acc.x, crgb[0]);
+        crgb[1] = fmaf(op, acc.y, crgb[1]);
+        crgb[2] = fmaf(op, acc.z, crgb[2]);
+        ca = fminf(fmaf(op, acc.w, ca), 1.f);
+      }
+    }
+
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    float dep = mp.clear_depth;
+    if (have) {
+      out = make_float4(crgb[0], crgb[1], crgb[2], ca);
+      // partials_to_canvas ray rebuild: delta_y runs along ru there
+      const float ex = view.dx_scale * (float)(2 * px - mp.width) * 0.5f;
+      const float ey = view.dy_scale * (float)(2 * py - mp.height) * 0.5f;
+      float q[3], qn = 0.f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        q[a] = view.look[a] + view.ru[a] * ex + view.ru[a] * ey;
+        qn = fmaf(q[a], q[a], qn);
+      }
+      const float qi = rsqrtf(qn);
+      float pos[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) pos[a] = fmaf(cdepth, q[a] * qi, view.origin[a]);
+      const float *M = view.projview;
+      const float z = M[8] * pos[0] + M[9] * pos[1] + M[10] * pos[2] + M[11];
+      const float wv = M[12] * pos[0] + M[13] * pos[1] + M[14] * pos[2] + M[15];
+      dep = 0.5f * (z / wv) + 0.49f;
+    }
+    if (mp.quantize_uint8) {
+      out.x = (float)(unsigned char)fminf(out.x * 255.f, 255.f) * (1.f / 255.f);
+      out.y = (float)(unsigned char)fminf(out.y * 255.f, 255.f) * (1.f / 255.f);
+      out.z = (float)(unsigned char)fminf(out.z * 255.f, 255.f) * (1.f / 255.f);
+      out.w = (float)(unsigned char)fminf(out.w * 255.f, 255.f) * (1.f / 255.f);
+      dep = fabsf(dep);
+    }
+    if (mp.render_bg) {
+      const float om = 1.f - out.w;
+      out.x = fmaf(mp.bg[0], om, out.x);
+      out.y = fmaf(mp.bg[1], om, out.y);
+      out.z = fmaf(mp.bg[2], om, out.z);
+      out.w = fmaf(mp.bg[3], om, out.w);
+    }
+    const int64_t pix = (int64_t)py * mp.width + px;
+    rgba[pix] = out;
+    depth[pix] = dep;
+  }
+  if (samples) {
+    unsigned long long c = (unsigned long long)count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0 && c) atomicAdd(samples, c);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
+                         const MarchParams &mp, const float4 *d_lut, float4 *d_rgba,
+                         float *d_depth, unsigned long long *d_samples,
+                         cudaStream_t stream)
+{
+  const size_t smem = sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(march_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float4) * kMaxLut +
+                                               sizeof(DomainDev) * kMaxDomains));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  dim3 grid((mp.width + kTile - 1) / kTile, (mp.height + kTile - 1) / kTile);
+  march_kernel<<<grid, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba,
+                                                 d_depth, d_samples);
+  return cudaGetLastError();
+}
+
+}  // namespace gvr

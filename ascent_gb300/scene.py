@@ -1,0 +1,187 @@
+"""Python handle over a device-resident gvr_scene (C ABI in include/gvr.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _field_args(field):
+    """(pointer, dtype code, keepalive, location, count) for numpy or torch input."""
+    try:
+        import torch
+    except ImportError:  # pragma: no cover - torch is always present here
+        torch = None
+    if torch is not None and isinstance(field, torch.Tensor):
+        if field.dtype not in (torch.float32, torch.float64):
+            raise N.GvrError(N.GVR_ERR_UNSUPPORTED, "field must be float32 or float64")
+        t = field.contiguous()
+        loc = N.MEM_DEVICE if t.is_cuda else N.MEM_HOST
+        code = N.DTYPE_FLOAT64 if t.dtype == torch.float64 else N.DTYPE_FLOAT32
+        return C.c_void_p(t.data_ptr()), code, t, loc, t.numel()
+    a = np.asarray(field)
+    if a.dtype not in (np.float32, np.float64):
+        a = a.astype(np.float32)
+    a = np.ascontiguousarray(a)
+    code = N.DTYPE_FLOAT64 if a.dtype == np.float64 else N.DTYPE_FLOAT32
+    return C.c_void_p(a.ctypes.data), code, a, N.MEM_HOST, a.size
+
+
+class Scene:
+    """Domains resident on one CUDA device, rendered by the fused march kernel."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        N.call("gvr_scene_create", int(device), C.byref(h))
+        self.handle = h
+        self.device = int(device)
+
+    def add_uniform(self, field, origin, spacing, association: int = N.ASSOC_VERTEX) -> int:
+        """field shaped (nz, ny, nx) nodes (or cells for element association)."""
+        shape = tuple(field.shape)
+        if len(shape) != 3:
+            raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "field must be 3D (nz, ny, nx)")
+        extra = 1 if association == N.ASSOC_ELEMENT else 0
+        dims = (C.c_int * 3)(shape[2] + extra, shape[1] + extra, shape[0] + extra)
+        o = (C.c_double * 3)(*map(float, origin))
+        s = (C.c_double * 3)(*map(float, spacing))
+        ptr, code, keep, loc, _ = _field_args(field)
+        did = C.c_int(-1)
+        N.call("gvr_scene_add_uniform", self.handle, dims, o, s, ptr, code, 1, int(association),
+               loc, C.byref(did))
+        del keep
+        return did.value
+
+    def add_rectilinear(self, field, x, y, z, association: int = N.ASSOC_VERTEX) -> int:
+        xs = [np.ascontiguousarray(c, dtype=np.float64) for c in (x, y, z)]
+        dims = (C.c_int * 3)(*[len(c) for c in xs])
+        ptr, code, keep, loc, _ = _field_args(field)
+        did = C.c_int(-1)
+        N.call("gvr_scene_add_rectilinear", self.handle, dims, N.dptr(xs[0]), N.dptr(xs[1]),
+               N.dptr(xs[2]), ptr, code, 1, int(association), loc, C.byref(did))
+        del keep
+        return did.value
+
+    def update_field(self, domain_id: int, field) -> None:
+        ptr, code, keep, loc, _ = _field_args(field)
+        N.call("gvr_scene_update_field", self.handle, int(domain_id), ptr, code, 1, loc)
+        del keep
+
+    @property
+    def num_domains(self) -> int:
+        n = C.c_int()
+        N.call("gvr_scene_num_domains", self.handle, C.byref(n))
+        return n.value
+
+    def bounds(self, domain_id: int = -1) -> np.ndarray:
+        b = np.zeros(6, dtype=np.float64)
+        N.call("gvr_scene_bounds", self.handle, int(domain_id), N.dptr(b))
+        return b
+
+    def scalar_range(self) -> np.ndarray:
+        r = np.zeros(2, dtype=np.float64)
+        N.call("gvr_scene_range", self.handle, N.dptr(r))
+        return r
+
+    def render(self, camera: N.Camera, params: N.RenderParams, *, device_out=False, stream=None,
+               count_samples=False):
+        """Render one view. Host numpy (H, W, 4)/(H, W) unless device_out, then torch CUDA tensors."""
+        w, h = params.width, params.height
+        n = C.c_uint64(0)
+        nptr = C.byref(n) if count_samples else None
+        st = C.c_void_p(stream) if stream is not None else None
+        if device_out:
+            import torch
+            rgba = torch.empty((h, w, 4), dtype=torch.float32, device=f"cuda:{self.device}")
+            depth = torch.empty((h, w), dtype=torch.float32, device=f"cuda:{self.device}")
+            if stream is None:
+                st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            N.call("gvr_render_volume", self.handle, C.byref(camera), C.byref(params),
+                   C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, st, nptr)
+        else:
+            rgba = np.empty((h, w, 4), dtype=np.float32)
+            depth = np.empty((h, w), dtype=np.float32)
+            N.call("gvr_render_volume", self.handle, C.byref(camera), C.byref(params),
+                   C.c_void_p(rgba.ctypes.data), C.c_void_p(depth.ctypes.data), N.MEM_HOST, st, nptr)
+        if count_samples:
+            return rgba, depth, int(n.value)
+        return rgba, depth
+
+    def close(self) -> None:
+        if self.handle:
+            N.lib().gvr_scene_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# host-logic helpers (thin wrappers over the C ABI)
+# ---------------------------------------------------------------------------
+
+def correct_opacity(alpha, num_samples: int) -> np.ndarray:
+    a = np.ascontiguousarray(alpha, dtype=np.float64)
+    out = np.empty_like(a)
+    N.call("gvr_correct_opacity", N.dptr(a), a.size, int(num_samples), N.dptr(out))
+    return out
+
+
+def sample_distance(bounds, num_samples: int) -> float:
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    d = C.c_float()
+    N.call("gvr_sample_distance", N.dptr(b), int(num_samples), C.byref(d))
+    return d.value
+
+
+def color_table_sample(rgb_pos, rgb, alpha_pos, alpha, n: int = 1024, uint8_mode: int = N.UINT8_NONE):
+    rp = np.ascontiguousarray(rgb_pos, dtype=np.float64)
+    rc = np.ascontiguousarray(rgb, dtype=np.float64).reshape(-1)
+    ap = np.ascontiguousarray(alpha_pos, dtype=np.float64)
+    av = np.ascontiguousarray(alpha, dtype=np.float64)
+    t = N.ColorTable(len(rp), N.dptr(rp), N.dptr(rc), len(ap), N.dptr(ap), N.dptr(av))
+    out = np.empty((n, 4), dtype=np.float32)
+    N.call("gvr_color_table_sample", C.byref(t), int(n), int(uint8_mode), N.fptr(out))
+    return out
+
+
+def camera_reset_to_bounds(bounds) -> N.Camera:
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    c = N.Camera()
+    N.call("gvr_camera_reset_to_bounds", C.byref(c), N.dptr(b))
+    return c
+
+
+def camera_azimuth(cam: N.Camera, deg: float) -> None:
+    N.call("gvr_camera_azimuth", C.byref(cam), float(deg))
+
+
+def camera_elevation(cam: N.Camera, deg: float) -> None:
+    N.call("gvr_camera_elevation", C.byref(cam), float(deg))
+
+
+def cinema_cameras(bounds, phi_theta) -> list:
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    pt = np.ascontiguousarray(phi_theta, dtype=np.float32).reshape(-1, 2)
+    out = (N.Camera * max(len(pt), 1))()
+    N.call("gvr_cinema_cameras", N.dptr(b), N.fptr(pt), len(pt), out)
+    return [out[i].copy() for i in range(len(pt))]
+
+
+def visibility_order(cam: N.Camera, domain_bounds) -> np.ndarray:
+    b = np.ascontiguousarray(domain_bounds, dtype=np.float64).reshape(-1, 6)
+    order = np.zeros(len(b), dtype=np.int32)
+    N.call("gvr_visibility_order", C.byref(cam), N.dptr(b), len(b),
+           order.ctypes.data_as(C.POINTER(C.c_int)))
+    return order

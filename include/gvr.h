@@ -1,0 +1,235 @@
+/*
+ * gvr.h — C ABI of the GB300 volume renderer (Ascent scene plot `type: volume`).
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns a gvr_status. The message of the last failing call on the calling
+ * host thread is available from gvr_last_error().
+ *
+ * Conventions shared by every call:
+ *   - Images are row-major, pixel_id = y * width + x, y pointing up (the
+ *     VTK-m canvas convention that VolumeRenderer.cpp:299-300 decodes).
+ *   - Colours are RGBA float32, premultiplied by alpha.
+ *   - Depth is the image-space depth 0.5 * z_ndc + 0.49 of the front-most
+ *     volume partial (src/libs/vtkh/rendering/VolumeRenderer.cpp:369-372);
+ *     pixels that no partial reaches keep gvr_render_params.clear_depth.
+ *   - `stream` is a cudaStream_t passed as void*; NULL means the legacy
+ *     default stream. Calls are stream-ordered; host outputs are complete
+ *     when the call returns.
+ *   - GVR_MEM_HOST / GVR_MEM_DEVICE say where a caller buffer lives.
+ */
+#ifndef GVR_H
+#define GVR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GVR_VERSION 1
+
+#if defined(GVR_BUILDING) && defined(__GNUC__)
+#define GVR_API __attribute__((visibility("default")))
+#else
+#define GVR_API
+#endif
+
+typedef enum gvr_status {
+  GVR_OK = 0,
+  GVR_ERR_INVALID_ARGUMENT = 1,
+  GVR_ERR_CUDA = 2,
+  GVR_ERR_OUT_OF_MEMORY = 3,
+  GVR_ERR_UNSUPPORTED = 4,
+  GVR_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+  GVR_ERR_NOT_FOUND = 6
+} gvr_status;
+
+enum { GVR_MEM_HOST = 0, GVR_MEM_DEVICE = 1 };
+enum { GVR_DTYPE_FLOAT32 = 0, GVR_DTYPE_FLOAT64 = 1 };
+enum { GVR_ASSOC_VERTEX = 0, GVR_ASSOC_ELEMENT = 1 };
+enum { GVR_DOMAIN_UNIFORM = 0, GVR_DOMAIN_RECTILINEAR = 1, GVR_DOMAIN_HEX = 2 };
+enum { GVR_LUT_NEAREST = 0, GVR_LUT_LINEAR = 1 };
+enum { GVR_UINT8_NONE = 0, GVR_UINT8_ROUND = 1, GVR_UINT8_TRUNCATE = 2 };
+
+/* A perspective camera (the state vtkm::rendering::Camera keeps in 3D mode,
+ * as set by parse_camera, ascent_runtime_conduit_to_vtkm_parsing.cpp:91-174).
+ * fov_y is in degrees; zoom is the multiplicative factor Ascent's `zoom` key
+ * gives after zoom_to_vtkm_zoom (conduit_to_vtkm_parsing.cpp:59-69), i.e.
+ * 1 means no zoom; xpan/ypan shift the image in normalised device units. */
+typedef struct gvr_camera {
+  float position[3];
+  float look_at[3];
+  float up[3];
+  float fov_y;
+  float zoom;
+  float xpan;
+  float ypan;
+  float near_plane;
+  float far_plane;
+} gvr_camera;
+
+/* Parameters of one volume render (VolumeRenderer::PreExecute and the
+ * per-domain wrappers, VolumeRenderer.cpp:93-284, 600-612). */
+typedef struct gvr_render_params {
+  int width;
+  int height;
+  float sample_dist;        /* world units between samples along a ray     */
+  float scalar_min;         /* m_range after Renderer::PreExecute          */
+  float scalar_max;
+  const float *lut_rgba;    /* host pointer, lut_size RGBA entries          */
+  int lut_size;             /* 1 .. 4096                                    */
+  int lut_filter;           /* GVR_LUT_NEAREST or GVR_LUT_LINEAR            */
+  float alpha_cull;         /* partials with alpha below this are dropped
+                               (0.001f, VolumeRenderer.cpp:271)             */
+  float early_term;         /* stop a ray once its alpha reaches this;
+                               >= 1 disables early termination              */
+  int quantize_uint8;       /* 1: round-trip the canvas through the uint8
+                               vtkh::Image (Image.hpp:102-105)              */
+  int render_bg;            /* blend bg_color behind the volume             */
+  float bg_color[4];
+  float clear_depth;        /* depth of pixels no partial reaches           */
+} gvr_render_params;
+
+/* A 1D colour/opacity transfer function given as control points
+ * (parse_color_table, conduit_to_vtkm_parsing.cpp:199-305). Positions are
+ * normalised scalars in [0,1], sorted ascending and unique. */
+typedef struct gvr_color_table {
+  int n_rgb;
+  const double *rgb_pos;    /* n_rgb positions                              */
+  const double *rgb;        /* 3 * n_rgb colours in [0,1]                   */
+  int n_alpha;
+  const double *alpha_pos;  /* n_alpha positions                            */
+  const double *alpha;      /* n_alpha opacities in [0,1]                   */
+} gvr_color_table;
+
+typedef struct gvr_scene gvr_scene;
+
+/* ------------------------------------------------------------------ */
+/* Library                                                              */
+/* ------------------------------------------------------------------ */
+
+/* Message of the last failing call on this host thread ("" if none). */
+GVR_API const char *gvr_last_error(void);
+
+/* GVR_VERSION of the loaded library. */
+GVR_API int gvr_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Host logic of the volume plot (no device work)                       */
+/* ------------------------------------------------------------------ */
+
+/* Opacity correction of every alpha control point:
+ * a' = 1 - (1 - a)^(10 / num_samples).
+ * Replaces VolumeRenderer::CorrectOpacity (VolumeRenderer.cpp:448-466).
+ * Errors: num_samples < 1 (VolumeRenderer::SetNumberOfSamples, :622-629). */
+GVR_API int gvr_correct_opacity(const double *alpha_in, int n, int num_samples,
+                        double *alpha_out);
+
+/* sample_dist = |extent(bounds)| / num_samples, bounds = {xmin,xmax,ymin,
+ * ymax,zmin,zmax}. Replaces VolumeRenderer::PreExecute (:600-612). */
+GVR_API int gvr_sample_distance(const double bounds[6], int num_samples,
+                        float *sample_dist);
+
+/* Sample the transfer function at n evenly spaced positions i/(n-1) into
+ * n RGBA floats. uint8_mode GVR_UINT8_ROUND/TRUNCATE passes every channel
+ * through an 8-bit value and back (x/255), as detail::convert_table does for
+ * the multi-domain path (VolumeRenderer.cpp:65-90, 1024 entries). */
+GVR_API int gvr_color_table_sample(const gvr_color_table *table, int n,
+                           int uint8_mode, float *rgba_out);
+
+/* Default camera for the scene bounds (vtkm Camera::ResetToBounds, called
+ * by vtkh::MakeRender, Render.cpp:314-347). */
+GVR_API int gvr_camera_reset_to_bounds(gvr_camera *camera, const double bounds[6]);
+
+/* Rotate the camera position about the view-up axis through look_at
+ * (parse_camera `azimuth`, conduit_to_vtkm_parsing.cpp:165-169). */
+GVR_API int gvr_camera_azimuth(gvr_camera *camera, double degrees);
+
+/* Rotate the camera position about the right axis through look_at
+ * (parse_camera `elevation`, conduit_to_vtkm_parsing.cpp:170-174). */
+GVR_API int gvr_camera_elevation(gvr_camera *camera, double degrees);
+
+/* Cinema sweep cameras: one camera per (phi, theta) pair in degrees,
+ * phi_theta holding 2*n floats. Replaces
+ * CinemaManager::create_cinema_cameras
+ * (ascent_runtime_rendering_filters.cpp:906-960). */
+GVR_API int gvr_cinema_cameras(const double bounds[6], const float *phi_theta, int n,
+                       gvr_camera *cameras_out);
+
+/* Visibility order of n domains for one camera: order[d] is the rank of
+ * domain d when domains are sorted by the distance from the camera to the
+ * centre of their bounds (6 doubles per domain). Replaces
+ * VolumeRenderer::FindVisibilityOrdering / FindMinDepth / DepthSort
+ * (VolumeRenderer.cpp:638-650, 691-831, 834-866). */
+GVR_API int gvr_visibility_order(const gvr_camera *camera, const double *domain_bounds,
+                         int n, int *order);
+
+/* ------------------------------------------------------------------ */
+/* Device-resident scene                                                */
+/* ------------------------------------------------------------------ */
+
+/* Create an empty scene whose domains live on CUDA device `device`.
+ * Replaces the vtkh::DataSet handed to VolumeRenderer::SetInput
+ * (VolumeRenderer.cpp:868-907). */
+GVR_API int gvr_scene_create(int device, gvr_scene **scene_out);
+GVR_API int gvr_scene_destroy(gvr_scene *scene);
+
+/* Add a uniform domain: dims = node counts (>= 2 each), origin/spacing
+ * cast to float32 as the Blueprint adapter does
+ * (ascent_vtkh_data_adapter.cpp:1177-1313). The scalar field has
+ * dims[0]*dims[1]*dims[2] values (vertex) or (dims-1) products (element),
+ * x fastest, `stride` elements apart (1 = contiguous), in `location`
+ * memory, float32 or float64 (AddField, :1782-2040). The field is copied
+ * into the scene's bricked device layout. */
+GVR_API int gvr_scene_add_uniform(gvr_scene *scene, const int dims[3],
+                          const double origin[3], const double spacing[3],
+                          const void *field, int dtype, int64_t stride,
+                          int association, int location, int *domain_id);
+
+/* Add a rectilinear domain with per-axis node coordinates x[dims[0]],
+ * y[dims[1]], z[dims[2]] (host, strictly increasing;
+ * RectilinearBlueprintToVTKmDataSet, ascent_vtkh_data_adapter.cpp:1318-1430). */
+GVR_API int gvr_scene_add_rectilinear(gvr_scene *scene, const int dims[3],
+                              const double *x, const double *y, const double *z,
+                              const void *field, int dtype, int64_t stride,
+                              int association, int location, int *domain_id);
+
+/* Replace the field of an existing domain (same size, type rules as the
+ * add call); the bricked copy and macrocell ranges are rebuilt on device. */
+GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *field,
+                           int dtype, int64_t stride, int location);
+
+GVR_API int gvr_scene_num_domains(const gvr_scene *scene, int *n);
+
+/* Bounds {xmin,xmax,ymin,ymax,zmin,zmax} of one domain, or of the whole
+ * scene when domain_id == -1 (DataSet::GetGlobalBounds). */
+GVR_API int gvr_scene_bounds(const gvr_scene *scene, int domain_id, double bounds[6]);
+
+/* Global scalar range {min,max} of the scene field (Renderer::PreExecute,
+ * Renderer.cpp:144-179). */
+GVR_API int gvr_scene_range(const gvr_scene *scene, double range[2]);
+
+/* ------------------------------------------------------------------ */
+/* Rendering                                                            */
+/* ------------------------------------------------------------------ */
+
+/* Render the scene's volume for one camera into rgba (4*W*H floats) and
+ * depth (W*H floats), both in `out_location` memory. Every structured
+ * domain is marched and the per-domain partials are composited per pixel
+ * by exit distance, front to back. Replaces VolumeRenderer::DoExecute with
+ * RenderOneDomainPerRank / RenderMultipleDomainsPerRank, the partial
+ * extraction, PartialCompositor::composite and partials_to_canvas
+ * (VolumeRenderer.cpp:141-391, 469-597; PartialCompositor.cpp:57-90,
+ * 244-547). `samples_out` (may be NULL) receives the number of samples the
+ * march evaluated. */
+GVR_API int gvr_render_volume(gvr_scene *scene, const gvr_camera *camera,
+                      const gvr_render_params *params, float *rgba,
+                      float *depth, int out_location, void *stream,
+                      uint64_t *samples_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GVR_H */

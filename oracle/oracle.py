@@ -1,0 +1,154 @@
+"""ctypes binding of the CPU oracle (``oracle/gvr_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: loaded by tests/, by ``__graft_entry__.smoke()``
+as the checker, and by bench.py's CPU-baseline arm. The product library
+never imports this module.
+
+Two builds of one C source:
+  precision=64 -> liboracle64.so, FP64 arithmetic (the accuracy oracle)
+  precision=32 -> liboracle32.so, FP32 arithmetic (the timed CPU port)
+and, when the reference sources are present at build time,
+``_ref/libapcomp_ref.so``: the reference's own partial compositor.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from ascent_gb300._native import Camera, ColorTable, RenderParams, dptr, fptr
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF = HERE / "_ref"
+REFERENCE_ROOT = Path(os.environ.get("GVR_REFERENCE_ROOT", "/root/reference"))
+
+PARTIAL_DTYPE = np.dtype([("pixel_id", "<i4"), ("depth", "<f4"), ("rgb", "<f4", (3,)),
+                          ("alpha", "<f4")])
+
+_libs: dict = {}
+
+
+def build(with_reference: bool | None = None) -> None:
+    """make the oracle; also the apcomp reference when its sources exist."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if with_reference is None:
+        with_reference = (REFERENCE_ROOT / "src/libs/apcomp/partial_compositor.cpp").exists()
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+
+
+def load(precision: int = 64) -> C.CDLL:
+    if precision in _libs:
+        return _libs[precision]
+    path = BUILD / f"liboracle{precision}.so"
+    if not path.exists():
+        build(with_reference=False)
+    lib = C.CDLL(str(path))
+    i, d, f, vp = C.c_int, C.c_double, C.c_float, C.c_void_p
+    P = C.POINTER
+    lib.or_correct_opacity.argtypes = [P(d), i, i, P(d)]
+    lib.or_sample_distance.argtypes = [P(d), i]
+    lib.or_sample_distance.restype = f
+    lib.or_color_table_sample.argtypes = [P(ColorTable), i, i, P(f)]
+    lib.or_camera_reset_to_bounds.argtypes = [P(Camera), P(d)]
+    lib.or_camera_azimuth.argtypes = [P(Camera), d]
+    lib.or_camera_elevation.argtypes = [P(Camera), d]
+    lib.or_cinema_cameras.argtypes = [P(d), P(f), i, P(Camera)]
+    lib.or_visibility_order.argtypes = [P(Camera), P(d), i, P(i)]
+    lib.or_composite_partials.argtypes = [i, P(i), vp, vp]
+    lib.or_scene_new.restype = vp
+    lib.or_scene_free.argtypes = [vp]
+    lib.or_scene_add_uniform.argtypes = [vp, P(i), P(d), P(d), P(f), i]
+    lib.or_scene_add_rectilinear.argtypes = [vp, P(i), P(d), P(d), P(d), P(f), i]
+    lib.or_render.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
+    lib.or_num_threads.restype = i
+    _libs[precision] = lib
+    return lib
+
+
+def load_apcomp_reference():
+    """The reference's compiled partial compositor, or None if it was not built."""
+    path = REF / "libapcomp_ref.so"
+    if not path.exists():
+        return None
+    lib = C.CDLL(str(path))
+    lib.ref_apcomp_composite.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_void_p, C.c_void_p]
+    lib.ref_apcomp_composite.restype = C.c_int
+    return lib
+
+
+def _ints(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class OracleScene:
+    """Domains as the oracle sees them; field arrays are kept alive here."""
+
+    def __init__(self, precision: int = 64):
+        self.lib = load(precision)
+        self.handle = self.lib.or_scene_new()
+        self._keep = []
+
+    def add_uniform(self, dims, origin, spacing, field, assoc=0) -> int:
+        dims_a, dims_p = _ints(dims)
+        o = np.ascontiguousarray(origin, dtype=np.float64)
+        s = np.ascontiguousarray(spacing, dtype=np.float64)
+        f = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        self._keep += [dims_a, o, s, f]
+        return self.lib.or_scene_add_uniform(self.handle, dims_p, dptr(o), dptr(s), fptr(f), int(assoc))
+
+    def add_rectilinear(self, x, y, z, field, assoc=0) -> int:
+        xs = [np.ascontiguousarray(c, dtype=np.float64) for c in (x, y, z)]
+        dims_a, dims_p = _ints([len(c) for c in xs])
+        f = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        self._keep += [dims_a, f, *xs]
+        return self.lib.or_scene_add_rectilinear(self.handle, dims_p, dptr(xs[0]), dptr(xs[1]),
+                                                 dptr(xs[2]), fptr(f), int(assoc))
+
+    def render(self, cam: Camera, params: RenderParams):
+        w, h = params.width, params.height
+        rgba = np.zeros((h, w, 4), dtype=np.float32)
+        depth = np.zeros((h, w), dtype=np.float32)
+        n = C.c_uint64(0)
+        rc = self.lib.or_render(self.handle, C.byref(cam), C.byref(params), fptr(rgba), fptr(depth),
+                                C.byref(n))
+        if rc != 0:
+            raise RuntimeError(f"oracle render failed with status {rc}")
+        return rgba, depth, int(n.value)
+
+    def close(self):
+        if self.handle:
+            self.lib.or_scene_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def composite_partials(images, precision: int = 64, reference: bool = False) -> np.ndarray:
+    """Composite a list of PARTIAL_DTYPE arrays; reference=True uses apcomp."""
+    counts_a, counts_p = _ints([len(im) for im in images])
+    flat = np.ascontiguousarray(np.concatenate(images) if images else np.zeros(0, PARTIAL_DTYPE),
+                                dtype=PARTIAL_DTYPE)
+    out = np.zeros(max(len(flat), 1), dtype=PARTIAL_DTYPE)
+    if reference:
+        lib = load_apcomp_reference()
+        if lib is None:
+            raise RuntimeError("apcomp reference library was not built")
+        n = lib.ref_apcomp_composite(len(images), counts_p, flat.ctypes.data, out.ctypes.data)
+    else:
+        n = load(precision).or_composite_partials(len(images), counts_p, flat.ctypes.data,
+                                                  out.ctypes.data)
+    return out[:n].copy()
+
+
+def num_threads(precision: int = 32) -> int:
+    return int(load(precision).or_num_threads())

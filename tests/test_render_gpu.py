@@ -1,0 +1,249 @@
+"""CUDA path vs the FP64 oracle, through the C ABI, on seeded inputs.
+
+Bar (per pixel, per RGBA channel): |error| <= 2/255 on >= 99.9% of pixels
+and mean absolute error <= 1e-3, against the oracle run with the same
+parameters (same early termination). The error against the oracle with
+early termination off is computed too and held to the same bar.
+"""
+import numpy as np
+import pytest
+
+from ascent_gb300 import _native as N
+from ascent_gb300 import scene as S
+from ascent_gb300 import volume as V
+from ascent_gb300 import workloads as W
+from oracle import oracle as O
+
+from conftest import assert_parity, image_error
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_scene(wl):
+    osc = O.OracleScene(64)
+    for d in wl.domains:
+        osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    return osc
+
+
+def render_both(wl, cam=None, **kw):
+    cam = cam or V.workload_camera(wl)
+    p = V.workload_params(wl, **kw)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        g_rgba, g_depth, g_n = sc.render(cam, p, count_samples=True)
+    o_rgba, o_depth, o_n = oracle_scene(wl).render(cam, p)
+    return (g_rgba, g_depth, g_n), (o_rgba, o_depth, o_n), p
+
+
+def test_plain_small_single_domain():
+    wl = W.plain_small(n=64, width=256, height=256)
+    (g, gd, gn), (o, od, on), p = render_both(wl)
+    assert p.quantize_uint8 == 1
+    e = assert_parity(g, o)
+    assert o[..., 3].max() > 0.2, "image must not be empty"
+    assert abs(gn - on) <= 1e-3 * on, (gn, on)
+    have = o[..., 3] > 0
+    np.testing.assert_allclose(gd[have], od[have], rtol=0, atol=1e-4)
+    np.testing.assert_array_equal(gd[~have], od[~have])
+
+
+def test_plain_cpu_case_512():
+    """The CPU-runnable plain case at its full size: 64^3, 512^2, 218 samples."""
+    wl = W.plain_small()
+    (g, gd, gn), (o, od, on), p = render_both(wl)
+    assert_parity(g, o)
+    (g2, _, _), (o2, _, _), _ = render_both(wl, early_term=1.0)
+    assert_parity(g2, o2)
+    assert_parity(g, o2)  # early termination at 0.99 stays within the bar
+
+
+def test_multi_domain_composite_uint8_lut():
+    wl = W.plain_small(n=49, width=200, height=150, parts=(2, 2, 2))
+    (g, gd, gn), (o, od, on), p = render_both(wl)
+    assert p.quantize_uint8 == 0
+    assert_parity(g, o)
+    assert abs(gn - on) <= 1e-3 * on
+    have = o[..., 3] > 0
+    np.testing.assert_allclose(gd[have], od[have], rtol=0, atol=2e-4)
+
+
+def test_multi_domain_uneven_split_matches_single_domain_geometry():
+    wl = W.plain_small(n=41, width=96, height=96, parts=(3, 1, 2))
+    (g, _, _), (o, _, _), _ = render_both(wl)
+    assert_parity(g, o)
+
+
+@pytest.mark.parametrize("az,el,zoom", [(0, 0, 1.0), (135, -40, 1.0), (200, 70, 2.0), (30, 20, 0.5)])
+def test_camera_variants(az, el, zoom):
+    wl = W.plain_small(n=33, width=128, height=96, parts=(2, 1, 1))
+    cam = S.camera_reset_to_bounds(wl.bounds)
+    S.camera_azimuth(cam, az)
+    S.camera_elevation(cam, el)
+    cam.zoom = zoom
+    (g, gd, _), (o, od, _), _ = render_both(wl, cam=cam)
+    assert_parity(g, o)
+
+
+def test_camera_inside_volume_and_looking_away():
+    wl = W.plain_small(n=33, width=64, height=64)
+    cam = S.camera_reset_to_bounds(wl.bounds)
+    cam.position[:] = [0.5, 0.5, 0.5]
+    cam.look_at[:] = [0.9, 0.6, 0.4]
+    (g, _, _), (o, _, _), _ = render_both(wl, cam=cam)
+    assert_parity(g, o)
+    cam.position[:] = [0.5, 0.5, 3.0]
+    cam.look_at[:] = [0.5, 0.5, 6.0]
+    (g, gd, gn), (o, od, on), p = render_both(wl, cam=cam)
+    assert gn == on == 0
+    assert np.all(g == 0) and np.all(gd == p.clear_depth)
+
+
+def test_odd_image_sizes_and_tiny_lut():
+    wl = W.plain_small(n=20, width=37, height=1)
+    (g, _, _), (o, _, _), _ = render_both(wl)
+    assert_parity(g, o)
+    wl = W.plain_small(n=20, width=1, height=1)
+    (g, _, _), (o, _, _), _ = render_both(wl)
+    assert_parity(g, o)
+    wl = W.plain_small(n=24, width=45, height=33)
+    lut = np.array([[0, 0, 1, 0.0], [1, 0.5, 0, 0.2]], np.float32)
+    cam = V.workload_camera(wl)
+    for filt in (N.LUT_NEAREST, N.LUT_LINEAR):
+        p = N.make_params(45, 33, 0.01, wl.scalar_range, lut, lut_filter=filt)
+        with S.Scene(0) as sc:
+            V.load_workload(sc, wl)
+            g, _ = sc.render(cam, p)
+        o, _, _ = oracle_scene(wl).render(cam, p)
+        assert_parity(g, o)
+
+
+def test_empty_space_skipping_is_exact():
+    """Bricks whose range maps to zero opacity are skipped; samples still count."""
+    wl = W.plain_small(n=72, width=128, height=128)
+    vr = V.workload_renderer(wl)
+    lut = vr.lut(True)
+    lut[: 600, 3] = 0.0  # transparent below s = 0.586
+    cam = V.workload_camera(wl)
+    p = N.make_params(128, 128, S.sample_distance(wl.bounds, 218), wl.scalar_range, lut)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        g, gd, gn = sc.render(cam, p, count_samples=True)
+    o, od, on = oracle_scene(wl).render(cam, p)
+    assert_parity(g, o)
+    assert abs(gn - on) <= 1e-3 * on
+
+
+def test_background_blend_and_depth_clear():
+    wl = W.plain_small(n=24, width=64, height=48, parts=(1, 2, 1))
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl, render_bg=True, bg_color=(0.1, 0.2, 0.3, 1.0))
+    p.clear_depth = 1.001
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        g, gd = sc.render(cam, p)
+    o, od, _ = oracle_scene(wl).render(cam, p)
+    assert_parity(g, o)
+    np.testing.assert_allclose(g[..., 3], 1.0, atol=1e-6)
+
+
+def test_rectilinear_domain_matches_oracle():
+    rng = np.random.default_rng(7)
+    xs = [np.cumsum(np.r_[0.0, rng.uniform(0.5, 1.5, n - 1)]) for n in (30, 25, 35)]
+    xs = [x / x[-1] for x in xs]
+    c, s, a = W.blob_params(rng)
+    f = W.blob_field(xs, c, s, a)
+    lut = V.VolumeRenderer().lut(True)
+    rp, rgb, ap, al = W.linear_ramp_tf()
+    vr = V.VolumeRenderer()
+    vr.set_color_table(V.TransferFunction(rp, rgb, ap, al))
+    vr.set_num_samples(150)
+    lut = vr.lut(True)
+    b = np.array([0, 1, 0, 1, 0, 1.0])
+    cam = S.camera_reset_to_bounds(b)
+    S.camera_azimuth(cam, 40)
+    S.camera_elevation(cam, 25)
+    p = N.make_params(120, 100, S.sample_distance(b, 150), (float(f.min()), float(f.max())), lut)
+    with S.Scene(0) as sc:
+        sc.add_rectilinear(f, *xs)
+        g, gd = sc.render(cam, p)
+    osc = O.OracleScene(64)
+    osc.add_rectilinear(*xs, f)
+    o, od, _ = osc.render(cam, p)
+    assert o[..., 3].max() > 0.1
+    assert_parity(g, o)
+
+
+def test_element_field_matches_oracle():
+    rng = np.random.default_rng(9)
+    cells = rng.uniform(0, 1, (15, 17, 19)).astype(np.float32)
+    rp, rgb, ap, al = W.linear_ramp_tf(alpha_max=0.8)
+    vr = V.VolumeRenderer()
+    vr.set_color_table(V.TransferFunction(rp, rgb, ap, al))
+    lut = vr.lut(True)
+    sp = (1 / 19, 1 / 17, 1 / 15)
+    b = np.array([0, 1, 0, 1, 0, 1.0])
+    cam = S.camera_reset_to_bounds(b)
+    S.camera_azimuth(cam, 10)
+    p = N.make_params(80, 80, S.sample_distance(b, 100), (0.0, 1.0), lut)
+    with S.Scene(0) as sc:
+        sc.add_uniform(cells, (0, 0, 0), sp, association=N.ASSOC_ELEMENT)
+        g, _ = sc.render(cam, p)
+    osc = O.OracleScene(64)
+    osc.add_uniform((20, 18, 16), (0, 0, 0), sp, cells, assoc=N.ASSOC_ELEMENT)
+    o, _, _ = osc.render(cam, p)
+    # nearest-cell lookups flip at cell faces under FP32 vs FP64 positions
+    e = image_error(g, o)
+    assert e["frac_within_2"] >= 0.99 and e["mae"] <= 2e-3, e
+
+
+def test_float64_and_strided_device_input():
+    import torch
+    wl = W.plain_small(n=24, width=64, height=64)
+    d = wl.domains[0]
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    with S.Scene(0) as sc:
+        sc.add_uniform(torch.from_numpy(d.field.astype(np.float64)).cuda(), d.origin, d.spacing)
+        g64, _ = sc.render(cam, p)
+    with S.Scene(0) as sc:
+        sc.add_uniform(torch.from_numpy(d.field).cuda(), d.origin, d.spacing)
+        g32, _ = sc.render(cam, p)
+        t, _ = sc.render(cam, p, device_out=True)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(t.cpu().numpy(), g32)
+    np.testing.assert_array_equal(g64, g32)
+
+
+def test_update_field_and_bounds_and_range():
+    wl = W.plain_small(n=24, width=48, height=48, parts=(2, 1, 1))
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        assert sc.num_domains == 2
+        np.testing.assert_allclose(sc.bounds(), wl.bounds, atol=1e-6)
+        lo, hi = sc.scalar_range()
+        assert np.isclose(lo, wl.scalar_range[0]) and np.isclose(hi, wl.scalar_range[1])
+        sc.update_field(1, wl.domains[1].field * 2)
+        assert np.isclose(sc.scalar_range()[1], max(wl.domains[0].field.max(), 2 * wl.domains[1].field.max()))
+        with pytest.raises(N.GvrError):
+            sc.update_field(5, wl.domains[0].field)
+
+
+def test_invalid_arguments_raise():
+    wl = W.plain_small(n=16, width=16, height=16)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        cam = V.workload_camera(wl)
+        p = V.workload_params(wl)
+        p.sample_dist = 0.0
+        with pytest.raises(N.GvrError):
+            sc.render(cam, p)
+        p = V.workload_params(wl)
+        bad = cam.copy()
+        bad.look_at[:] = list(bad.position)
+        with pytest.raises(N.GvrError):
+            sc.render(bad, p)
+        with pytest.raises(N.GvrError):
+            sc.add_uniform(np.zeros((1, 4, 4), np.float32), (0, 0, 0), (1, 1, 1))
+        with pytest.raises(N.GvrError):
+            sc.add_uniform(np.full((4, 4, 4), np.nan, np.float32), (0, 0, 0), (1, 1, 1))
