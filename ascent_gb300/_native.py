@@ -104,6 +104,7 @@ _lock = threading.Lock()
 _SIGS = {
     "gvr_last_error": (C.c_char_p, []),
     "gvr_version": (C.c_int, []),
+    "gvr_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
     "gvr_correct_opacity": (C.c_int, [C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "gvr_sample_distance": (C.c_int, [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_float)]),
     "gvr_color_table_sample": (C.c_int, [C.POINTER(ColorTable), C.c_int, C.c_int, C.POINTER(C.c_float)]),
@@ -157,3 +158,9 @@ def check(rc: int) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(lib(), name)(*args))
+
+
+def launch_count() -> int:
+    n = C.c_uint64(0)
+    call("gvr_launch_count", C.byref(n))
+    return int(n.value)

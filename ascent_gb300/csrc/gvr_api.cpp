@@ -5,6 +5,7 @@
 // distance, transfer-function sampling, cameras, visibility order, domain
 // bookkeeping) plus the orchestration of the device kernels.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -15,6 +16,7 @@
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
 constexpr double kPi = 3.14159265358979323846;
 }  // namespace
 
@@ -25,6 +27,10 @@ int set_error(int code, const std::string &msg)
   g_last_error = msg;
   return code;
 }
+
+void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int cuda_error(cudaError_t e, const char *what)
 {
@@ -154,6 +160,13 @@ using namespace gvr;
 extern "C" {
 
 const char *gvr_last_error(void) { return g_last_error.c_str(); }
+
+int gvr_launch_count(uint64_t *n)
+{
+  if (!n) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = launch_count();
+  return GVR_OK;
+}
 
 int gvr_version(void) { return GVR_VERSION; }
 
@@ -325,6 +338,8 @@ static void free_domain(Domain &d)
   for (int a = 0; a < 3; ++a) cudaFree(d.d_coord[a]);
   cudaFree(d.d_brick_range);
   cudaFree(d.d_brick_empty);
+  cudaFree(d.stg.buf);
+  cudaFree(d.stg.block_range);
   d = Domain();
 }
 
@@ -354,15 +369,16 @@ static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, i
   cudaError_t e;
   if (d.dev.assoc == GVR_ASSOC_VERTEX) {
     e = launch_brick_field(field, dtype, stride, location == GVR_MEM_DEVICE, d.dev.dims,
-                           d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, 0);
+                           d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, d.stg, 0);
   } else {
     e = launch_cells_field(field, dtype, stride, location == GVR_MEM_DEVICE, (int64_t)d.n_values,
-                           d.d_cells, d.range, 0);
+                           d.d_cells, d.range, d.stg, 0);
   }
   if (e != cudaSuccess) return cuda_error(e, "field upload");
   if (!(std::isfinite(d.range[0]) && std::isfinite(d.range[1])))
     return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
   s->table_dirty = true;
+  s->classify_valid = false;
   return GVR_OK;
 }
 
@@ -615,15 +631,28 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
   mp.clear_depth = p->clear_depth;
   for (int c = 0; c < 4; ++c) mp.bg[c] = p->bg_color[c];
 
-  e = cudaMemcpyAsync(s->d_lut, p->lut_rgba, sizeof(float4) * p->lut_size, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_error(e, "copy LUT");
-  // empty-space skipping: classify bricks against this transfer function
+  // empty-space skipping: classify bricks against this transfer function,
+  // unless the LUT, filter, range and fields are those of the last render
   mp.skip_empty = 1;
-  for (Domain &d : s->domains) {
-    if (d.dev.assoc != GVR_ASSOC_VERTEX) continue;
-    e = launch_empty_bricks(d.d_brick_range, d.n_bricks, s->d_lut, p->lut_size, p->lut_filter,
-                            mp.scalar_min, mp.inv_range, d.d_brick_empty, st);
-    if (e != cudaSuccess) return cuda_error(e, "empty-brick pass");
+  const size_t lut_floats = (size_t)p->lut_size * 4;
+  const bool same = s->classify_valid && s->classify_lut.size() == lut_floats &&
+                    s->classify_filter == p->lut_filter && s->classify_smin == mp.scalar_min &&
+                    s->classify_inv_range == mp.inv_range &&
+                    std::memcmp(s->classify_lut.data(), p->lut_rgba, lut_floats * sizeof(float)) == 0;
+  if (!same) {
+    e = cudaMemcpyAsync(s->d_lut, p->lut_rgba, sizeof(float4) * p->lut_size, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(e, "copy LUT");
+    for (Domain &d : s->domains) {
+      if (d.dev.assoc != GVR_ASSOC_VERTEX) continue;
+      e = launch_empty_bricks(d.d_brick_range, d.n_bricks, s->d_lut, p->lut_size, p->lut_filter,
+                              mp.scalar_min, mp.inv_range, d.d_brick_empty, st);
+      if (e != cudaSuccess) return cuda_error(e, "empty-brick pass");
+    }
+    s->classify_lut.assign(p->lut_rgba, p->lut_rgba + lut_floats);
+    s->classify_filter = p->lut_filter;
+    s->classify_smin = mp.scalar_min;
+    s->classify_inv_range = mp.inv_range;
+    s->classify_valid = true;
   }
   if (samples_out) {
     e = cudaMemsetAsync(s->d_counters, 0, sizeof(unsigned long long), st);

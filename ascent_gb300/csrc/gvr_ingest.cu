@@ -128,22 +128,29 @@ __global__ void empty_kernel(const float2 *__restrict__ brick_range, int64_t n,
   }
 }
 
+// Device-side source of a field upload: the caller's pointer when it is
+// device memory, else the domain's staging buffer (grown once, reused by
+// every later upload) filled from the host.
 cudaError_t stage_source(const void *src, int dtype, int64_t stride,
                          int src_on_device, int64_t n, const void **dsrc,
-                         void **owned, cudaStream_t stream)
+                         Staging &stg, cudaStream_t stream)
 {
-  *owned = nullptr;
   if (src_on_device) {
     *dsrc = src;
     return cudaSuccess;
   }
   const size_t esz = dtype == GVR_DTYPE_FLOAT64 ? 8 : 4;
   const size_t bytes = (size_t)((n - 1) * stride + 1) * esz;
-  cudaError_t e = cudaMalloc(owned, bytes);
-  if (e != cudaSuccess) return e;
-  e = cudaMemcpyAsync(*owned, src, bytes, cudaMemcpyHostToDevice, stream);
-  *dsrc = *owned;
-  return e;
+  if (bytes > stg.bytes) {
+    cudaFree(stg.buf);
+    stg.buf = nullptr;
+    stg.bytes = 0;
+    cudaError_t e = cudaMalloc(&stg.buf, bytes);
+    if (e != cudaSuccess) return e;
+    stg.bytes = bytes;
+  }
+  *dsrc = stg.buf;
+  return cudaMemcpyAsync(stg.buf, src, bytes, cudaMemcpyHostToDevice, stream);
 }
 
 }  // namespace
@@ -152,24 +159,23 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, const int dims[3],
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
-                               cudaStream_t stream)
+                               Staging &stg, cudaStream_t stream)
 {
   const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
   const void *dsrc = nullptr;
-  void *owned = nullptr;
-  cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, &owned, stream);
+  cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, stg, stream);
   if (e != cudaSuccess) return e;
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
   brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1],
                                                  dims[2], nbrick[0], nbrick[1], d_bricks,
                                                  d_brick_range);
+  count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   std::vector<float2> h((size_t)nb);
   e = cudaMemcpyAsync(h.data(), d_brick_range, sizeof(float2) * nb,
                       cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  if (owned) cudaFree(owned);
   if (e != cudaSuccess) return e;
   double lo = INFINITY, hi = -INFINITY;
   for (const float2 &r : h) {
@@ -184,25 +190,25 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
 
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, int64_t n, float *d_cells,
-                               double range_out[2], cudaStream_t stream)
+                               double range_out[2], Staging &stg, cudaStream_t stream)
 {
   const void *dsrc = nullptr;
-  void *owned = nullptr;
-  cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, &owned, stream);
+  cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, stg, stream);
   if (e != cudaSuccess) return e;
   int blocks = (int)((n + 255) / 256);
   if (blocks > 4096) blocks = 4096;
-  float2 *d_br = nullptr;
-  e = cudaMalloc(&d_br, sizeof(float2) * blocks);
-  if (e != cudaSuccess) { if (owned) cudaFree(owned); return e; }
+  if (!stg.block_range) {
+    e = cudaMalloc(&stg.block_range, sizeof(float2) * 4096);
+    if (e != cudaSuccess) return e;
+  }
+  float2 *d_br = stg.block_range;
   convert_kernel<<<blocks, 256, 0, stream>>>(dsrc, dtype, stride, n, d_cells, d_br);
+  count_launch();
   e = cudaGetLastError();
   std::vector<float2> h(blocks);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(h.data(), d_br, sizeof(float2) * blocks, cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  cudaFree(d_br);
-  if (owned) cudaFree(owned);
   if (e != cudaSuccess) return e;
   double lo = INFINITY, hi = -INFINITY;
   for (const float2 &r : h) {
@@ -225,6 +231,7 @@ cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
   if (blocks > 1216) blocks = 1216;
   empty_kernel<<<blocks, 256, 0, stream>>>(brick_range, n_bricks, d_lut, lut_size,
                                            lut_filter, scalar_min, inv_range, brick_empty);
+  count_launch();
   return cudaGetLastError();
 }
 

@@ -72,6 +72,14 @@ struct MarchParams {
   float bg[4];
 };
 
+// Reusable device buffers of one domain's field uploads: the staging copy
+// of a host field and the per-CTA ranges of the element-field reduction.
+struct Staging {
+  void *buf = nullptr;
+  size_t bytes = 0;
+  float2 *block_range = nullptr;
+};
+
 // Host-side record of a domain owned by a scene.
 struct Domain {
   DomainDev dev;
@@ -84,6 +92,7 @@ struct Domain {
   float2 *d_brick_range = nullptr;
   uint8_t *d_brick_empty = nullptr;
   int64_t n_bricks = 0;
+  Staging stg;
 };
 
 }  // namespace gvr
@@ -99,6 +108,12 @@ struct gvr_scene {
   float *d_depth_tmp = nullptr;
   int64_t tmp_pixels = 0;
   bool table_dirty = true;
+  // empty-brick classification of the last render, reused while the LUT,
+  // its filter and the scalar range stay the same and no field changed
+  bool classify_valid = false;
+  std::vector<float> classify_lut;
+  float classify_smin = 0.f, classify_inv_range = 0.f;
+  int classify_filter = -1;
 };
 
 namespace gvr {
@@ -110,15 +125,20 @@ int cuda_error(cudaError_t e, const char *what);
 // camera -> per-view constants (gvr_api.cpp)
 void make_view(const gvr_camera &cam, int width, int height, ViewDev *v);
 
+// kernels launched by this library since it was loaded
+void count_launch(int n = 1);
+uint64_t launch_count();
+
 // ingest kernels (gvr_ingest.cu)
 cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, const int dims[3],
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
-                               cudaStream_t stream);
+                               Staging &stg, cudaStream_t stream);
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, int64_t n, float *d_cells,
-                               double range_out[2], cudaStream_t stream);
+                               double range_out[2], Staging &stg,
+                               cudaStream_t stream);
 cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
                                 const float4 *d_lut, int lut_size, int lut_filter,
                                 float scalar_min, float inv_range,

@@ -342,6 +342,7 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
   dim3 grid((mp.width + kTile - 1) / kTile, (mp.height + kTile - 1) / kTile);
   march_kernel<<<grid, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba,
                                                  d_depth, d_samples);
+  count_launch();
   return cudaGetLastError();
 }
 

@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""Benchmark of Ascent's volume plot on GB300: samples/s of the fused march.
+
+Workload (default): a 513^3-node float32 field (Gaussian blobs + 3-octave
+sinusoidal turbulence, seed 2) split into 8 domains of 256^3 cells that share
+face nodes, rendered at 1024x1024 with visibility-ordered compositing,
+1774 samples over the bounds diagonal (0.5 cell), 256-point linear transfer
+function (opacity 0 -> 0.3), camera reset to the bounds then azimuth 30,
+elevation 20.
+
+A step is one render of that view. Reported:
+  value   Gsamples/s with the bricked field resident in HBM and the image
+          written to device memory (CUDA events on the launching stream).
+  e2e     the same metric through the C ABI with HOST buffers: every step
+          uploads the 8 fields from pinned host memory (re-bricking them)
+          and reads the RGBA + depth image back.
+  roofline  algorithmic bytes (32 B per sample + 20 B per pixel) per launch
+          over the march kernel's event-timed duration, against the measured
+          HBM copy bandwidth.
+  cpu_baseline  the FP32 OpenMP port of the oracle on this host's cores,
+          timed on a band of image rows of the same view.
+
+--impl reference runs that CPU implementation alone (rank 0), each step a
+bounded band of rows, and prints the same JSON keys.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+BYTES_PER_SAMPLE = 32     # 8 float32 trilinear corners
+BYTES_PER_PIXEL = 20      # RGBA float32 + depth float32
+METRIC = "volume render Gsamples/s (512^3 in 8 domains, 1024^2)"
+UNIT = "Gsamples/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cells", type=int, default=512, help="cells per axis of the whole grid")
+    ap.add_argument("--size", type=int, default=1024, help="image width = height")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU time of the cpu_baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(samples: int, pixels: int):
+    """DRAM bytes per launch of the march kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "march_kernel_ncu.md"
+    if not f.exists():
+        return None, None
+    kv = {}
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            kv["t"] = float(line.split(":", 1)[1])
+        if line.startswith("traffic_workload:"):
+            kv["w"] = line.split(":", 1)[1].strip()
+    return kv.get("t"), kv.get("w")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def bricked_bytes(wl) -> int:
+    """Device bytes of the bricked fields: 736 floats per 8^3-cell brick."""
+    total = 0
+    for d in wl.domains:
+        nb = 1
+        for n in d.dims:
+            nb *= (n - 1 + 7) // 8
+        total += nb * 736 * 4
+    return total
+
+
+def setup_workload(args):
+    from ascent_gb300 import workloads as W
+    t = time.time()
+    wl = W.plain_large(n_cells=args.cells, width=args.size, height=args.size)
+    return wl, time.time() - t
+
+
+def bench_params(wl):
+    """Float 1024-entry LUT (see config["lut"]), no uint8 canvas round trip."""
+    from ascent_gb300 import _native as N
+    from ascent_gb300 import volume as V
+    vr = V.workload_renderer(wl)
+    lut = vr.lut(single_domain=True)          # float LUT
+    return vr.params(wl.width, wl.height, wl.bounds, wl.scalar_range, single_domain=False, lut=lut), N
+
+
+def cpu_sample(wl, cam, params, seconds: float, per_step: bool = False):
+    """Time the FP32 OpenMP oracle port on central row bands until `seconds` pass."""
+    from oracle import oracle as O
+    osc = O.OracleScene(32)
+    for d in wl.domains:
+        osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    h, w = params.height, params.width
+    rgba = np.zeros((h, w, 4), np.float32)
+    depth = np.zeros((h, w), np.float32)
+    band = 8
+    row = h // 2 - band // 2
+    samples = rows = 0
+    t0 = time.perf_counter()
+    while True:
+        r0 = row % h
+        r1 = min(r0 + band, h)
+        samples += osc.render_rows(cam, params, r0, r1, rgba, depth)
+        rows += r1 - r0
+        row = r1 if r1 < h else 0
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": samples / dt / 1e9, "unit": UNIT, "cores": O.num_threads(32), "kind": "port",
+            "sample": f"{rows} of {h} image rows (central bands) of the same view, "
+                      f"{samples} samples in {dt:.1f} s, FP32 OpenMP port of the oracle"}, osc
+
+
+def run_reference(args):
+    """CPU implementation of the path (the oracle's FP32 OpenMP port) on this host."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from ascent_gb300 import volume as V
+    wl, _ = setup_workload(args)
+    cam = V.workload_camera(wl)
+    params, _ = bench_params(wl)
+    from oracle import oracle as O
+    osc = O.OracleScene(32)
+    for d in wl.domains:
+        osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    h, w = params.height, params.width
+    rgba = np.zeros((h, w, 4), np.float32)
+    depth = np.zeros((h, w), np.float32)
+    budget = min(2.0, 150.0 / max(1, args.steps + args.warmup))
+    # calibrate a band height that takes about `budget` seconds
+    t0 = time.perf_counter()
+    osc.render_rows(cam, params, h // 2 - 2, h // 2 + 2, rgba, depth)
+    per_row = max((time.perf_counter() - t0) / 4, 1e-4)
+    band = int(max(1, min(h, budget / per_row)))
+    r0 = max(0, h // 2 - band // 2)
+    for _ in range(args.warmup):
+        osc.render_rows(cam, params, r0, r0 + band, rgba, depth)
+    total = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        total += osc.render_rows(cam, params, r0, r0 + band, rgba, depth)
+    dt = time.perf_counter() - t0
+    value = total / dt / 1e9
+    cores = O.num_threads(32)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": wl.name, "domains": len(wl.domains), "image": [w, h],
+                       "samples_param": wl.samples, "step_sample_rows": [r0, r0 + band]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"rows {r0}..{r0 + band} of {h} per step; the reference's "
+                                       "VTK-m renderer is not buildable here, this is the oracle's "
+                                       "FP32 OpenMP port of the same algorithm"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    from ascent_gb300 import _native as N
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import volume as V
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = local
+
+    wl, gen_s = setup_workload(args)
+    cam = V.workload_camera(wl)
+    params, _ = bench_params(wl)
+    pixels = wl.width * wl.height
+    scene = S.Scene(dev)
+    V.load_workload(scene, wl)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    # sample count of this view (deterministic), then warm-up
+    _, _, n_samples = scene.render(cam, params, device_out=True, stream=sptr, count_samples=True)
+    for _ in range(max(args.warmup, 3)):
+        scene.render(cam, params, device_out=True, stream=sptr)
+    torch.cuda.synchronize()
+
+    rgba = torch.empty((wl.height, wl.width, 4), dtype=torch.float32, device=f"cuda:{dev}")
+    depth = torch.empty((wl.height, wl.width), dtype=torch.float32, device=f"cuda:{dev}")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    import ctypes as C
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = N.launch_count()
+    for i in range(args.steps):
+        starts[i].record(stream)
+        N.call("gvr_render_volume", scene.handle, C.byref(cam), C.byref(params),
+               C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()), N.MEM_DEVICE,
+               C.c_void_p(sptr), None)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    launches = N.launch_count() - launches0
+    if dist:
+        dist.barrier()
+    per = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = starts[0].elapsed_time(ends[-1])
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # end to end: host fields -> C ABI (upload + re-brick) -> render -> host image
+    host_fields = [torch.from_numpy(d.field).pin_memory() for d in wl.domains]
+    h_rgba = torch.empty((wl.height, wl.width, 4), dtype=torch.float32).pin_memory()
+    h_depth = torch.empty((wl.height, wl.width), dtype=torch.float32).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+
+    def e2e_step():
+        for i, f in enumerate(host_fields):
+            N.call("gvr_scene_update_field", scene.handle, i, C.c_void_p(f.data_ptr()),
+                   N.DTYPE_FLOAT32, 1, N.MEM_HOST)
+        N.call("gvr_render_volume", scene.handle, C.byref(cam), C.byref(params),
+               C.c_void_p(h_rgba.data_ptr()), C.c_void_p(h_depth.data_ptr()), N.MEM_HOST, None, None)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank != 0:
+        return 0
+    pk = peaks()
+    avg_launch_s = statistics.mean(per) / 1e3
+    alg_bytes = n_samples * BYTES_PER_SAMPLE + pixels * BYTES_PER_PIXEL
+    achieved = alg_bytes / avg_launch_s / 1e9
+    traffic, traffic_wl = ncu_traffic(n_samples, pixels)
+    value = world * n_samples * args.steps / (total_ms / 1e3) / 1e9
+    e2e_value = world * n_samples * e2e_steps / e2e_s / 1e9
+    field_bytes = sum(d.field.nbytes for d in wl.domains)
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu, _ = cpu_sample(wl, cam, params, args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "fps": 1e3 * args.steps / total_ms,
+        "config": {"workload": wl.name, "grid_nodes": args.cells + 1, "domains": len(wl.domains),
+                   "image": [wl.width, wl.height], "samples_param": wl.samples,
+                   "sample_dist": params.sample_dist, "samples_per_frame": n_samples,
+                   "early_term": params.early_term,
+                   "lut": "1024-entry float LUT for both arms; the reference's multi-domain "
+                          "uint8 LUT would round opacity to 0 below s=0.98 at 1774 samples",
+                   "l2": f"inputs {bricked_bytes(wl) / 2**20:.0f} MiB bricked > 129 MB L2; "
+                         "not flushed",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "generate_s": round(gen_s, 2)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                     "peak_source": pk["source"], "traffic_workload": traffic_wl,
+                     "avg_launch_ms": avg_launch_s * 1e3,
+                     "algorithmic_bytes_per_launch": alg_bytes},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": field_bytes,
+                "d2h_bytes_per_step": pixels * BYTES_PER_PIXEL,
+                "steps": e2e_steps, "ms_per_step": e2e_s / e2e_steps * 1e3},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    scene.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

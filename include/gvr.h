@@ -115,6 +115,10 @@ GVR_API const char *gvr_last_error(void);
 /* GVR_VERSION of the loaded library. */
 GVR_API int gvr_version(void);
 
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (a diagnostic; no counterpart in the reference). */
+GVR_API int gvr_launch_count(uint64_t *n);
+
 /* ------------------------------------------------------------------ */
 /* Host logic of the volume plot (no device work)                       */
 /* ------------------------------------------------------------------ */

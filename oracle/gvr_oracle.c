@@ -670,20 +670,23 @@ static int cmp_rpartial(const void *pa, const void *pb)
   return a->dom - b->dom;
 }
 
-/* Render the scene for one camera. rgba: 4*W*H floats, depth: W*H floats.
+/* Render image rows [row0, row1) of the scene for one camera into full-size
+ * buffers (rgba: 4*W*H floats, depth: W*H floats; other rows untouched).
  * *samples_out (if non-NULL) receives the number of samples taken. */
-int or_render(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
-              float *rgba, float *depth, uint64_t *samples_out)
+int or_render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
+                   int row0, int row1, float *rgba, float *depth, uint64_t *samples_out)
 {
   const int W = p->width, H = p->height;
   if (W < 1 || H < 1 || !p->lut_rgba || p->lut_size < 2) return GVR_ERR_INVALID_ARGUMENT;
+  if (row0 < 0) row0 = 0;
+  if (row1 > H) row1 = H;
   or_basis b = make_basis(cam, W, H);
   double M[4][4];
   projview(cam, W, H, M);
   const int nd = s->n;
   uint64_t total = 0;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
-  for (int j = 0; j < H; ++j) {
+  for (int j = row0; j < row1; ++j) {
     or_rpartial *parts = (or_rpartial *)malloc(sizeof(or_rpartial) * (nd > 0 ? nd : 1));
     for (int i = 0; i < W; ++i) {
       v3 dir = add(b.look,
@@ -747,6 +750,13 @@ int or_render(const or_scene *s, const gvr_camera *cam, const gvr_render_params 
   }
   if (samples_out) *samples_out = total;
   return GVR_OK;
+}
+
+/* Render the whole image. */
+int or_render(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
+              float *rgba, float *depth, uint64_t *samples_out)
+{
+  return or_render_rows(s, cam, p, 0, p->height, rgba, depth, samples_out);
 }
 
 /* Number of OpenMP threads the render loop uses (1 without OpenMP). */

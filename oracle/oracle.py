@@ -65,6 +65,7 @@ def load(precision: int = 64) -> C.CDLL:
     lib.or_scene_add_uniform.argtypes = [vp, P(i), P(d), P(d), P(f), i]
     lib.or_scene_add_rectilinear.argtypes = [vp, P(i), P(d), P(d), P(d), P(f), i]
     lib.or_render.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
+    lib.or_render_rows.argtypes = [vp, P(Camera), P(RenderParams), i, i, P(f), P(f), P(C.c_uint64)]
     lib.or_num_threads.restype = i
     _libs[precision] = lib
     return lib
@@ -120,6 +121,15 @@ class OracleScene:
         if rc != 0:
             raise RuntimeError(f"oracle render failed with status {rc}")
         return rgba, depth, int(n.value)
+
+    def render_rows(self, cam: Camera, params: RenderParams, row0: int, row1: int, rgba, depth) -> int:
+        """Render rows [row0, row1) into caller buffers; returns the sample count."""
+        n = C.c_uint64(0)
+        rc = self.lib.or_render_rows(self.handle, C.byref(cam), C.byref(params), int(row0), int(row1),
+                                     fptr(rgba), fptr(depth), C.byref(n))
+        if rc != 0:
+            raise RuntimeError(f"oracle render failed with status {rc}")
+        return int(n.value)
 
     def close(self):
         if self.handle:
