@@ -350,6 +350,7 @@ int gvr_scene_destroy(gvr_scene *s)
   for (Domain &d : s->domains) free_domain(d);
   cudaFree(s->d_domains);
   cudaFree(s->d_lut);
+  cudaFree(s->d_any_empty);
   cudaFree(s->d_counters);
   cudaFree(s->d_rgba_tmp);
   cudaFree(s->d_depth_tmp);
@@ -440,6 +441,12 @@ static int add_structured(gvr_scene *s, int kind, const int dims[3], const doubl
   if (assoc == GVR_ASSOC_VERTEX) {
     d.n_values = (size_t)dims[0] * dims[1] * dims[2];
     d.n_bricks = (int64_t)d.dev.nbrick[0] * d.dev.nbrick[1] * d.dev.nbrick[2];
+    if (d.n_bricks * kBrickFloats >= (int64_t)1 << 31) {
+      free_domain(d);
+      return set_error(GVR_ERR_UNSUPPORTED,
+                       "a domain's bricked field must hold < 2^31 floats (about 1290^3 nodes); "
+                       "split it into more domains");
+    }
     e = cudaMalloc(&d.d_bricks, sizeof(float) * kBrickFloats * d.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&d.d_brick_range, sizeof(float2) * d.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&d.d_brick_empty, d.n_bricks);
@@ -489,6 +496,19 @@ int gvr_scene_update_field(gvr_scene *s, int domain_id, const void *field, int d
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
   return upload_field(s, s->domains[domain_id], field, dtype, stride, location);
+}
+
+int gvr_scene_set_tuning(gvr_scene *s, int packet_w, int unroll, int min_blocks)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if ((packet_w != 4 && packet_w != 8 && packet_w != 16) || (unroll != 1 && unroll != 2) ||
+      (min_blocks != 3 && min_blocks != 4))
+    return set_error(GVR_ERR_INVALID_ARGUMENT,
+                     "tuning: packet_w in {4,8,16}, unroll in {1,2}, min_blocks in {3,4}");
+  s->tuning.packet_w = packet_w;
+  s->tuning.unroll = unroll;
+  s->tuning.min_blocks = min_blocks;
+  return GVR_OK;
 }
 
 int gvr_scene_num_domains(const gvr_scene *s, int *n)
@@ -564,8 +584,16 @@ static int ensure_buffers(gvr_scene *s, int64_t pixels, int lut_size)
       if (e != cudaSuccess) return cuda_error(e, "cudaMalloc domain table");
       s->d_domains_cap = kMaxDomains;
     }
+    if (!s->d_any_empty) {
+      e = cudaMalloc(&s->d_any_empty, sizeof(int) * kMaxDomains);
+      if (e == cudaSuccess) e = cudaMemset(s->d_any_empty, 0, sizeof(int) * kMaxDomains);
+      if (e != cudaSuccess) return cuda_error(e, "cudaMalloc empty flags");
+    }
     std::vector<DomainDev> h(s->domains.size());
-    for (size_t i = 0; i < h.size(); ++i) h[i] = s->domains[i].dev;
+    for (size_t i = 0; i < h.size(); ++i) {
+      h[i] = s->domains[i].dev;
+      h[i].any_empty = s->d_any_empty + i;
+    }
     if (!h.empty()) {
       e = cudaMemcpy(s->d_domains, h.data(), sizeof(DomainDev) * h.size(), cudaMemcpyHostToDevice);
       if (e != cudaSuccess) return cuda_error(e, "copy domain table");
@@ -641,11 +669,13 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
                     std::memcmp(s->classify_lut.data(), p->lut_rgba, lut_floats * sizeof(float)) == 0;
   if (!same) {
     e = cudaMemcpyAsync(s->d_lut, p->lut_rgba, sizeof(float4) * p->lut_size, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_any_empty, 0, sizeof(int) * kMaxDomains, st);
     if (e != cudaSuccess) return cuda_error(e, "copy LUT");
-    for (Domain &d : s->domains) {
+    for (size_t i = 0; i < s->domains.size(); ++i) {
+      Domain &d = s->domains[i];
       if (d.dev.assoc != GVR_ASSOC_VERTEX) continue;
       e = launch_empty_bricks(d.d_brick_range, d.n_bricks, s->d_lut, p->lut_size, p->lut_filter,
-                              mp.scalar_min, mp.inv_range, d.d_brick_empty, st);
+                              mp.scalar_min, mp.inv_range, d.d_brick_empty, s->d_any_empty + i, st);
       if (e != cudaSuccess) return cuda_error(e, "empty-brick pass");
     }
     s->classify_lut.assign(p->lut_rgba, p->lut_rgba + lut_floats);
@@ -663,7 +693,7 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
   float4 *d_rgba = out_location == GVR_MEM_DEVICE ? (float4 *)rgba : s->d_rgba_tmp;
   float *d_depth = out_location == GVR_MEM_DEVICE ? depth : s->d_depth_tmp;
   e = launch_march(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
-                   samples_out ? s->d_counters : nullptr, st);
+                   samples_out ? s->d_counters : nullptr, s->tuning, st);
   if (e != cudaSuccess) return cuda_error(e, "march kernel launch");
   if (out_location == GVR_MEM_HOST) {
     e = cudaMemcpyAsync(rgba, d_rgba, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, st);

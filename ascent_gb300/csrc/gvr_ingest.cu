@@ -108,7 +108,7 @@ convert_kernel(const void *__restrict__ src, int dtype, int64_t stride, int64_t 
 __global__ void empty_kernel(const float2 *__restrict__ brick_range, int64_t n,
                              const float4 *__restrict__ lut, int lut_size,
                              int lut_filter, float smin, float inv_range,
-                             uint8_t *__restrict__ empty)
+                             uint8_t *__restrict__ empty, int *__restrict__ any_empty)
 {
   for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < n;
        b += (int64_t)gridDim.x * blockDim.x) {
@@ -125,6 +125,7 @@ __global__ void empty_kernel(const float2 *__restrict__ brick_range, int64_t n,
     for (int i = i0; i <= i1; ++i)
       if (lut[i].w > 0.f) { e = 0; break; }
     empty[b] = e;
+    if (e) *any_empty = 1;
   }
 }
 
@@ -224,13 +225,14 @@ cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
 cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
                                 const float4 *d_lut, int lut_size, int lut_filter,
                                 float scalar_min, float inv_range,
-                                uint8_t *brick_empty, cudaStream_t stream)
+                                uint8_t *brick_empty, int *any_empty, cudaStream_t stream)
 {
   if (n_bricks == 0) return cudaSuccess;
   int blocks = (int)((n_bricks + 255) / 256);
   if (blocks > 1216) blocks = 1216;
   empty_kernel<<<blocks, 256, 0, stream>>>(brick_range, n_bricks, d_lut, lut_size,
-                                           lut_filter, scalar_min, inv_range, brick_empty);
+                                           lut_filter, scalar_min, inv_range, brick_empty,
+                                           any_empty);
   count_launch();
   return cudaGetLastError();
 }

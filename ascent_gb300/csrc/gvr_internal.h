@@ -39,6 +39,16 @@ struct DomainDev {
   const float *coord[3];  // rectilinear node coordinates
   const float2 *brick_range;  // per-brick {min, max} of the field
   const uint8_t *brick_empty; // per-brick 1 = LUT alpha is 0 over its range
+  const int *any_empty;       // 1 if any brick of this domain is empty
+};
+
+// Launch shape of the march kernel (picked by the autotuner): pixel packet
+// width per warp (4, 8 or 16; height 32 / width), samples located per loop
+// iteration (1 or 2) and the CTAs per SM the register budget targets (3, 4).
+struct Tuning {
+  int packet_w = 8;
+  int unroll = 2;
+  int min_blocks = 4;
 };
 
 // Everything the march kernel needs for one view.
@@ -103,6 +113,8 @@ struct gvr_scene {
   gvr::DomainDev *d_domains = nullptr;   // device copy of the domain table
   int d_domains_cap = 0;
   float4 *d_lut = nullptr;               // LUT of the last render
+  int *d_any_empty = nullptr;            // per-domain empty-brick flags
+  gvr::Tuning tuning;
   unsigned long long *d_counters = nullptr;  // [0] samples
   float4 *d_rgba_tmp = nullptr;          // device image for host outputs
   float *d_depth_tmp = nullptr;
@@ -142,12 +154,14 @@ cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
 cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
                                 const float4 *d_lut, int lut_size, int lut_filter,
                                 float scalar_min, float inv_range,
-                                uint8_t *brick_empty, cudaStream_t stream);
+                                uint8_t *brick_empty, int *any_empty,
+                                cudaStream_t stream);
 
 // march kernel (gvr_march.cu)
 cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          const MarchParams &mp, const float4 *d_lut,
                          float4 *d_rgba, float *d_depth,
-                         unsigned long long *d_samples, cudaStream_t stream);
+                         unsigned long long *d_samples, const Tuning &tuning,
+                         cudaStream_t stream);
 
 }  // namespace gvr

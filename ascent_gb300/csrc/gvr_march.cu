@@ -26,7 +26,7 @@ namespace gvr {
 namespace {
 
 constexpr int kTile = 16;     // CTA tile edge in pixels
-constexpr int kThreads = 256; // 8 warps, each an 8x4 packet
+constexpr int kThreads = 256; // 8 warps, each a 32-ray packet
 
 struct Ray {
   float o[3];
@@ -197,12 +197,92 @@ __device__ int march_domain(const DomainDev &dm, const Ray &r, float t0, float t
   return count;
 }
 
-__global__ void __launch_bounds__(kThreads)
+
+// Uniform grid, vertex field, no empty bricks: the hot path. UNROLL samples
+// are located and their 8 corners loaded before any of them is blended, so
+// a warp keeps UNROLL x 8 loads in flight. Blending stays sequential and
+// stops exactly where the one-sample loop stops.
+template <int UNROLL>
+__device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, float t0,
+                                             float t1, const MarchParams &mp,
+                                             const float4 *lut, float thr, float4 &acc)
+{
+  const float dt = mp.sample_dist;
+  float A[3], B[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    A[a] = (r.o[a] - dm.origin[a]) * dm.inv_spacing[a];
+    B[a] = r.d[a] * dm.inv_spacing[a];
+  }
+  const int cmax[3] = {dm.dims[0] - 2, dm.dims[1] - 2, dm.dims[2] - 2};
+  const int sy = dm.nbrick[0] * kBrickFloats;
+  const int sz = dm.nbrick[1] * sy;
+  const float *__restrict__ bricks = dm.bricks;
+  const float nm1 = (float)(mp.lut_size - 1);
+  int count = 0;
+  for (int k = 0;; k += UNROLL) {
+    float v[UNROLL];
+    bool ok[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      float t = fmaf((float)(k + u), dt, t0);
+      ok[u] = t < t1;
+      t = ok[u] ? t : t0;
+      int off = 0;
+      float w[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float g = fmaf(t, B[a], A[a]);
+        const int c = max(0, min((int)g, cmax[a]));
+        w[a] = g - (float)c;
+        const int hi = c >> 3, lo = c & 7;
+        off += a == 0 ? hi * kBrickFloats + lo
+                      : (a == 1 ? hi * sy + lo * kBrickNodes : hi * sz + lo * kBrickNodes * kBrickNodes);
+      }
+      const float *p = bricks + off;
+      const float v000 = __ldg(p), v100 = __ldg(p + 1);
+      const float v010 = __ldg(p + kBrickNodes), v110 = __ldg(p + kBrickNodes + 1);
+      const float v001 = __ldg(p + kBrickNodes * kBrickNodes);
+      const float v101 = __ldg(p + kBrickNodes * kBrickNodes + 1);
+      const float v011 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
+      const float v111 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+      const float c00 = lerpf(v000, v100, w[0]);
+      const float c10 = lerpf(v010, v110, w[0]);
+      const float c01 = lerpf(v001, v101, w[0]);
+      const float c11 = lerpf(v011, v111, w[0]);
+      v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      if (!ok[u]) return count;
+      ++count;
+      const float s = __saturatef((v[u] - mp.scalar_min) * mp.inv_range);
+      float4 col;
+      if (mp.lut_filter == GVR_LUT_LINEAR) {
+        col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, s);
+      } else {
+        col = lut[min((int)(s * nm1), mp.lut_size - 1)];
+      }
+      const float wa = (1.f - acc.w) * col.w;
+      acc.x = fmaf(wa, col.x, acc.x);
+      acc.y = fmaf(wa, col.y, acc.y);
+      acc.z = fmaf(wa, col.z, acc.z);
+      acc.w += wa;
+      if (acc.w >= thr) return count;
+    }
+  }
+}
+
+// PW x (32 / PW) pixel packet per warp, 16 x 16 pixels per CTA.
+template <int PW, int UNROLL, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
 march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
              const MarchParams mp, const float4 *__restrict__ g_lut,
              float4 *__restrict__ rgba, float *__restrict__ depth,
              unsigned long long *__restrict__ samples)
 {
+  constexpr int PH = 32 / PW;
+  constexpr int PX = kTile / PW;  // packets per tile row
   extern __shared__ float4 smem[];
   float4 *lut = smem;
   DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
@@ -216,10 +296,9 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
   __syncthreads();
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int px = blockIdx.x * kTile + (warp & 1) * 8 + (lane & 7);
-  const int py = blockIdx.y * kTile + (warp >> 1) * 4 + (lane >> 3);
+  const int px = blockIdx.x * kTile + (warp % PX) * PW + (lane % PW);
+  const int py = blockIdx.y * kTile + (warp / PX) * PH + (lane / PW);
   const bool valid = px < mp.width && py < mp.height;
-
   int count = 0;
   if (valid) {
     Ray r;
@@ -259,7 +338,12 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
       last_d = best;
       const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      count += march_domain(doms[best], r, bt0, bt1, mp, lut, thr, acc);
+      const DomainDev &dm = doms[best];
+      if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
+          !(mp.skip_empty && *dm.any_empty))
+        count += march_uniform<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
+      else
+        count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
       if (acc.w < mp.alpha_cull) continue;
       if (!have) {
         crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
@@ -324,24 +408,42 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
 
 }  // namespace
 
+namespace {
+
+using MarchFn = void (*)(const DomainDev *, const ViewDev, const MarchParams, const float4 *,
+                         float4 *, float *, unsigned long long *);
+
+template <int PW, int UNROLL, int MINB>
+MarchFn pick() { return march_kernel<PW, UNROLL, MINB>; }
+
+MarchFn select(const Tuning &t)
+{
+  const int u = t.unroll >= 2 ? 2 : 1;
+  const int m = t.min_blocks >= 4 ? 4 : 3;
+  switch (t.packet_w) {
+    case 4:
+      return u == 2 ? (m == 4 ? pick<4, 2, 4>() : pick<4, 2, 3>()) : (m == 4 ? pick<4, 1, 4>() : pick<4, 1, 3>());
+    case 16:
+      return u == 2 ? (m == 4 ? pick<16, 2, 4>() : pick<16, 2, 3>()) : (m == 4 ? pick<16, 1, 4>() : pick<16, 1, 3>());
+    default:
+      return u == 2 ? (m == 4 ? pick<8, 2, 4>() : pick<8, 2, 3>()) : (m == 4 ? pick<8, 1, 4>() : pick<8, 1, 3>());
+  }
+}
+
+}  // namespace
+
 cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          const MarchParams &mp, const float4 *d_lut, float4 *d_rgba,
-                         float *d_depth, unsigned long long *d_samples,
+                         float *d_depth, unsigned long long *d_samples, const Tuning &tuning,
                          cudaStream_t stream)
 {
   const size_t smem = sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(march_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(float4) * kMaxLut +
-                                               sizeof(DomainDev) * kMaxDomains));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  MarchFn fn = select(tuning);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(float4) * kMaxLut + sizeof(DomainDev) * kMaxDomains));
+  if (e != cudaSuccess) return e;
   dim3 grid((mp.width + kTile - 1) / kTile, (mp.height + kTile - 1) / kTile);
-  march_kernel<<<grid, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba,
-                                                 d_depth, d_samples);
+  fn<<<grid, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba, d_depth, d_samples);
   count_launch();
   return cudaGetLastError();
 }

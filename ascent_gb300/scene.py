@@ -69,6 +69,11 @@ class Scene:
         N.call("gvr_scene_update_field", self.handle, int(domain_id), ptr, code, 1, loc)
         del keep
 
+    def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4) -> None:
+        """Launch shape of the march kernel; images do not depend on it."""
+        N.call("gvr_scene_set_tuning", self.handle, int(packet_w), int(unroll), int(min_blocks))
+        self.tuning = (int(packet_w), int(unroll), int(min_blocks))
+
     @property
     def num_domains(self) -> int:
         n = C.c_int()

@@ -1,0 +1,85 @@
+"""Autotuner for the march kernel's launch shape.
+
+Candidates are the shapes gvr_scene_set_tuning accepts: pixel packet width
+per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1 or 2)
+and the CTAs per SM the register budget targets (3 or 4). Every candidate
+renders the caller's own view on the caller's scene; the fastest median of
+a few CUDA-event-timed launches wins. Images do not depend on the shape, so
+tuning never changes results. Winners are cached per (GPU, workload key) in
+a JSON file so later runs skip the search.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+import json
+import os
+import statistics
+from pathlib import Path
+
+from . import _native as N
+
+CANDIDATES = [dict(packet_w=p, unroll=u, min_blocks=m)
+              for p, u, m in itertools.product((8, 4, 16), (2, 1), (3, 4))]
+CACHE = Path(os.environ.get("GVR_TUNE_CACHE", Path.home() / ".cache" / "gvr_tune.json"))
+
+
+def _key(scene, params) -> str:
+    import torch
+    name = torch.cuda.get_device_name(scene.device).replace(" ", "_")
+    return f"{name}|dom{scene.num_domains}|{params.width}x{params.height}|lut{params.lut_size}"
+
+
+def _time(scene, camera, params, rgba, depth, stream, reps: int) -> float:
+    import torch
+    sptr = C.c_void_p(stream.cuda_stream)
+    args = (scene.handle, C.byref(camera), C.byref(params), C.c_void_p(rgba.data_ptr()),
+            C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, sptr, None)
+    N.call("gvr_render_volume", *args)  # warm
+    times = []
+    for _ in range(reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        N.call("gvr_render_volume", *args)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return statistics.median(times)
+
+
+def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True) -> dict:
+    """Pick and set the fastest launch shape for this scene and view; returns
+    {"best": shape, "ms": {shape-string: median ms}, "cached": bool}."""
+    import torch
+    key = _key(scene, params)
+    cache = {}
+    if use_cache and CACHE.exists():
+        try:
+            cache = json.loads(CACHE.read_text())
+        except Exception:
+            cache = {}
+    if use_cache and key in cache:
+        best = cache[key]["best"]
+        scene.set_tuning(**best)
+        return {"best": best, "ms": cache[key].get("ms", {}), "cached": True}
+    dev = f"cuda:{scene.device}"
+    rgba = torch.empty((params.height, params.width, 4), dtype=torch.float32, device=dev)
+    depth = torch.empty((params.height, params.width), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(scene.device)
+    results = {}
+    for cand in CANDIDATES:
+        scene.set_tuning(**cand)
+        results[f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}"] = (
+            _time(scene, camera, params, rgba, depth, stream, reps), cand)
+    name, (ms, best) = min(results.items(), key=lambda kv: kv[1][0])
+    scene.set_tuning(**best)
+    out = {"best": best, "ms": {k: round(v[0], 4) for k, v in results.items()}, "cached": False}
+    if use_cache:
+        try:
+            CACHE.parent.mkdir(parents=True, exist_ok=True)
+            cache[key] = {"best": best, "ms": out["ms"]}
+            CACHE.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+    return out

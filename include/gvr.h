@@ -206,6 +206,14 @@ GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *
 
 GVR_API int gvr_scene_num_domains(const gvr_scene *scene, int *n);
 
+/* Launch shape of the scene's march kernel: pixel packet width per warp
+ * (4, 8 or 16; the packet is 32 rays), samples located per loop iteration
+ * (1 or 2) and CTAs per SM targeted by the register budget (3 or 4).
+ * Results do not depend on it. Set by the autotuner (ascent_gb300.tune);
+ * no counterpart in the reference. */
+GVR_API int gvr_scene_set_tuning(gvr_scene *scene, int packet_w, int unroll,
+                                 int min_blocks);
+
 /* Bounds {xmin,xmax,ymin,ymax,zmin,zmax} of one domain, or of the whole
  * scene when domain_id == -1 (DataSet::GetGlobalBounds). */
 GVR_API int gvr_scene_bounds(const gvr_scene *scene, int domain_id, double bounds[6]);

@@ -251,3 +251,26 @@ def test_invalid_arguments_raise():
             sc.add_uniform(np.zeros((1, 4, 4), np.float32), (0, 0, 0), (1, 1, 1))
         with pytest.raises(N.GvrError):
             sc.add_uniform(np.full((4, 4, 4), np.nan, np.float32), (0, 0, 0), (1, 1, 1))
+
+
+def test_every_launch_shape_gives_the_same_image():
+    from ascent_gb300 import tune
+    wl = W.plain_small(n=57, width=100, height=84, parts=(2, 2, 1))
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        ref = None
+        for cand in tune.CANDIDATES:
+            sc.set_tuning(**cand)
+            g, gd, n = sc.render(cam, p, count_samples=True)
+            if ref is None:
+                ref = (g, gd, n)
+                continue
+            np.testing.assert_allclose(g, ref[0], rtol=0, atol=1e-6)
+            np.testing.assert_array_equal(gd, ref[1])
+            assert n == ref[2]
+        out = tune.autotune(sc, cam, p, reps=1, use_cache=False)
+        assert out["best"] in tune.CANDIDATES and len(out["ms"]) == len(tune.CANDIDATES)
+        with pytest.raises(N.GvrError):
+            sc.set_tuning(packet_w=5)
