@@ -240,6 +240,33 @@ GVR_API int gvr_render_volume(gvr_scene *scene, const gvr_camera *camera,
                       float *depth, int out_location, void *stream,
                       uint64_t *samples_out);
 
+/* Render one uniform domain without allocating any device memory; no
+ * counterpart in the reference. For callers that may not call cudaMalloc or
+ * cudaFree — typically a simulation that gives all GPU memory to its own
+ * pool allocator, where a library allocation can fail against the pool's
+ * budget and cudaMalloc/cudaFree would synchronise the device under the
+ * simulation's streams.
+ *
+ * `field` is a device pointer to dims[0]*dims[1]*dims[2] float32 node values
+ * (x fastest); `rgba` (4*W*H floats) and `depth` (W*H floats) are device
+ * pointers; all must live on the calling thread's current CUDA device. The
+ * result equals gvr_render_volume on a scene holding this one domain.
+ * `samples_out` (may be NULL) is a host pointer; when given, the call waits
+ * for the render to finish.
+ *
+ * Scratch: the device copy of the LUT and the sample counter live in one
+ * fixed 64 KiB + 256 B array inside the library, which every GPU that loads
+ * the library holds until the process exits. lut_size above 4096 is
+ * rejected. The first call on a device looks up that array's device address
+ * (set-up), so make the first call on each device before any stream
+ * capture. Every call shares the array: calls that overlap on the GPU race
+ * on it, so serialise them (one stream, or wait between calls). */
+GVR_API int gvr_render_uniform_noalloc(const float *field, const int dims[3],
+                                       const double origin[3], const double spacing[3],
+                                       const gvr_camera *camera,
+                                       const gvr_render_params *params, float *rgba,
+                                       float *depth, void *stream, uint64_t *samples_out);
+
 #ifdef __cplusplus
 }
 #endif
