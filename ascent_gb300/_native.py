@@ -121,6 +121,12 @@ _SIGS = {
     "gvr_scene_add_rectilinear": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p,
                                             C.c_int, C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "gvr_scene_add_hex": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_int64, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                    C.c_int, C.POINTER(C.c_int)]),
+    "gvr_scene_hex_bvh": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]),
+    "gvr_scene_hex_locate": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "gvr_scene_update_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int64, C.c_int]),
     "gvr_scene_num_domains": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "gvr_scene_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),

@@ -340,6 +340,7 @@ static void free_domain(Domain &d)
   cudaFree(d.d_brick_empty);
   cudaFree(d.stg.buf);
   cudaFree(d.stg.block_range);
+  free_hex(d);
   d = Domain();
 }
 
@@ -368,6 +369,13 @@ static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, i
   if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
     return set_error(GVR_ERR_INVALID_ARGUMENT, "bad field location");
   cudaError_t e;
+  if (d.dev.kind == GVR_DOMAIN_HEX) {
+    const int rc = hex_update_field(d, field, dtype, stride, location);
+    if (rc != GVR_OK) return rc;
+    s->table_dirty = true;
+    s->classify_valid = false;
+    return GVR_OK;
+  }
   if (d.dev.assoc == GVR_ASSOC_VERTEX) {
     e = launch_brick_field(field, dtype, stride, location == GVR_MEM_DEVICE, d.dev.dims,
                            d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, d.stg, 0);
@@ -693,7 +701,7 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
   float4 *d_rgba = out_location == GVR_MEM_DEVICE ? (float4 *)rgba : s->d_rgba_tmp;
   float *d_depth = out_location == GVR_MEM_DEVICE ? depth : s->d_depth_tmp;
   e = launch_march(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
-                   samples_out ? s->d_counters : nullptr, s->tuning, st);
+                   samples_out ? s->d_counters : nullptr, s->tuning, s->has_hex, st);
   if (e != cudaSuccess) return cuda_error(e, "march kernel launch");
   if (out_location == GVR_MEM_HOST) {
     e = cudaMemcpyAsync(rgba, d_rgba, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, st);

@@ -1,0 +1,165 @@
+// gvr_hex_device.cuh — point location in hexahedral meshes (device code).
+//
+// A point is located by walking the mesh's LBVH (flat layout written by
+// gvr_hex.cu) and, at each candidate leaf, solving the inverse trilinear
+// map x(r,s,t) = p by Newton's method. This is the algorithm of Devil Ray's
+// DeviceMesh::locate (src/libs/dray/data_model/device_mesh.hpp:250-360: a
+// stack walk that enters the left child first, pushes the right one when the
+// point is inside both boxes, and stops at the first leaf whose element
+// contains the point) with its NewtonSolve (src/libs/dray/newton_solver.hpp:
+// 33-110, at most 10 steps). Arithmetic is FP32.
+//
+// Flat BVH node (4 float4 per inner node):
+//   [0] = left.lo.x, left.lo.y, left.lo.z, left.hi.x
+//   [1] = left.hi.y, left.hi.z, right.lo.x, right.lo.y
+//   [2] = right.lo.z, right.hi.x, right.hi.y, right.hi.z
+//   [3] = bits of int left child, bits of int right child, 0, 0
+// A child >= 0 is an inner node index; a child < 0 is leaf k = -child - 1
+// (k indexes the Morton-sorted leaves; hex_ids[k] is its cell id).
+#pragma once
+
+#include "gvr_internal.h"
+
+namespace gvr {
+
+constexpr int kHexNewtonSteps = 10;        // NewtonSolve default_max_steps
+constexpr float kHexNewtonTol = 1e-5f;     // |step|_inf in reference space
+constexpr float kHexInsideTol = 1e-4f;     // r, s, t in [-tol, 1 + tol]
+constexpr int kHexStack = 64;
+
+__device__ __forceinline__ void hex_load(const DomainDev &dm, int cell, float4 (&v)[8])
+{
+  const int4 a = __ldg(dm.hex_conn + 2 * (int64_t)cell);
+  const int4 b = __ldg(dm.hex_conn + 2 * (int64_t)cell + 1);
+  v[0] = __ldg(dm.hex_nodes + a.x);
+  v[1] = __ldg(dm.hex_nodes + a.y);
+  v[2] = __ldg(dm.hex_nodes + a.z);
+  v[3] = __ldg(dm.hex_nodes + a.w);
+  v[4] = __ldg(dm.hex_nodes + b.x);
+  v[5] = __ldg(dm.hex_nodes + b.y);
+  v[6] = __ldg(dm.hex_nodes + b.z);
+  v[7] = __ldg(dm.hex_nodes + b.w);
+}
+
+// Trilinear shape-function weights for VTK hex order at (r, s, t).
+__device__ __forceinline__ void hex_weights(float r, float s, float t, float (&n)[8])
+{
+  const float r0 = 1.f - r, s0 = 1.f - s, t0 = 1.f - t;
+  n[0] = r0 * s0 * t0;
+  n[1] = r * s0 * t0;
+  n[2] = r * s * t0;
+  n[3] = r0 * s * t0;
+  n[4] = r0 * s0 * t;
+  n[5] = r * s0 * t;
+  n[6] = r * s * t;
+  n[7] = r0 * s * t;
+}
+
+// Newton's method on x(r,s,t) - p = 0 from the guess in rst; true when it
+// converged inside the element (rst then holds the reference coordinates).
+__device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3], float rst[3])
+{
+  float r = rst[0], s = rst[1], t = rst[2];
+  bool conv = false;
+  for (int it = 0; it < kHexNewtonSteps; ++it) {
+    const float r0 = 1.f - r, s0 = 1.f - s, t0 = 1.f - t;
+    float n[8];
+    hex_weights(r, s, t, n);
+    // derivative weights
+    const float dr[8] = {-s0 * t0, s0 * t0, s * t0, -s * t0, -s0 * t, s0 * t, s * t, -s * t};
+    const float ds[8] = {-r0 * t0, -r * t0, r * t0, r0 * t0, -r0 * t, -r * t, r * t, r0 * t};
+    const float dt[8] = {-r0 * s0, -r * s0, -r * s, -r0 * s, r0 * s0, r * s0, r * s, r0 * s};
+    float F[3] = {-p[0], -p[1], -p[2]};
+    float J[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const float x[3] = {v[i].x, v[i].y, v[i].z};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        F[a] = fmaf(n[i], x[a], F[a]);
+        J[a][0] = fmaf(dr[i], x[a], J[a][0]);
+        J[a][1] = fmaf(ds[i], x[a], J[a][1]);
+        J[a][2] = fmaf(dt[i], x[a], J[a][2]);
+      }
+    }
+    // solve J d = F by the adjugate
+    const float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    if (!(fabsf(det) > 0.f)) return false;
+    const float id = 1.f / det;
+    const float c10 = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    const float c11 = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    const float c12 = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    const float c20 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    const float c21 = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    const float c22 = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const float d0 = (c00 * F[0] + c10 * F[1] + c20 * F[2]) * id;
+    const float d1 = (c01 * F[0] + c11 * F[1] + c21 * F[2]) * id;
+    const float d2 = (c02 * F[0] + c12 * F[1] + c22 * F[2]) * id;
+    r -= d0;
+    s -= d1;
+    t -= d2;
+    if (!(fabsf(r) < 1e3f && fabsf(s) < 1e3f && fabsf(t) < 1e3f)) return false;
+    if (fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2))) < kHexNewtonTol) {
+      conv = true;
+      break;
+    }
+  }
+  rst[0] = r;
+  rst[1] = s;
+  rst[2] = t;
+  return conv && r >= -kHexInsideTol && r <= 1.f + kHexInsideTol && s >= -kHexInsideTol &&
+         s <= 1.f + kHexInsideTol && t >= -kHexInsideTol && t <= 1.f + kHexInsideTol;
+}
+
+__device__ __forceinline__ bool in_box(const float p[3], float lx, float ly, float lz, float hx,
+                                       float hy, float hz)
+{
+  return !(p[0] < lx || p[1] < ly || p[2] < lz || p[0] > hx || p[1] > hy || p[2] > hz);
+}
+
+// Locate p: returns the cell id (or -1) and fills rst and the cell's corners.
+__device__ __forceinline__ int hex_locate(const DomainDev &dm, const float p[3], float rst[3],
+                                          float4 (&v)[8])
+{
+  if (dm.n_cells == 1) {
+    hex_load(dm, 0, v);
+    rst[0] = rst[1] = rst[2] = 0.5f;
+    return hex_newton(v, p, rst) ? 0 : -1;
+  }
+  int stack[kHexStack];
+  int sp = 0;
+  int node = 0;
+  for (;;) {
+    if (node >= 0) {
+      const float4 *q = dm.hex_bvh + 4 * (int64_t)node;
+      const float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), ch = __ldg(q + 3);
+      const bool inl = in_box(p, a.x, a.y, a.z, a.w, b.x, b.y);
+      const bool inr = in_box(p, b.z, b.w, c.x, c.y, c.z, c.w);
+      if (!inl && !inr) {
+        if (sp == 0) return -1;
+        node = stack[--sp];
+        continue;
+      }
+      const int lc = __float_as_int(ch.x), rc = __float_as_int(ch.y);
+      if (inl && inr) {
+        if (sp < kHexStack) stack[sp++] = rc;
+        node = lc;
+      } else {
+        node = inl ? lc : rc;
+      }
+    } else {
+      const int k = -node - 1;
+      const int cell = __ldg(dm.hex_ids + k);
+      hex_load(dm, cell, v);
+      rst[0] = rst[1] = rst[2] = 0.5f;
+      if (hex_newton(v, p, rst)) return cell;
+      if (sp == 0) return -1;
+      node = stack[--sp];
+    }
+  }
+}
+
+}  // namespace gvr

@@ -40,6 +40,13 @@ struct DomainDev {
   const float2 *brick_range;  // per-brick {min, max} of the field
   const uint8_t *brick_empty; // per-brick 1 = LUT alpha is 0 over its range
   const int *any_empty;       // 1 if any brick of this domain is empty
+  // hexahedral domains
+  const float4 *hex_nodes;    // x, y, z, vertex field value
+  const int4 *hex_conn;       // 8 node ids per cell (VTK hex order), 2 int4
+  const float4 *hex_bvh;      // 4 float4 per inner node (see gvr_hex.cu)
+  const int *hex_ids;         // cell id of each sorted leaf
+  int n_cells;
+  int pad_;
 };
 
 // Launch shape of the march kernel (picked by the autotuner): pixel packet
@@ -103,6 +110,19 @@ struct Domain {
   uint8_t *d_brick_empty = nullptr;
   int64_t n_bricks = 0;
   Staging stg;
+  // hexahedral domains (device)
+  int64_t n_nodes = 0;
+  int64_t n_cells = 0;
+  float4 *d_nodes = nullptr;
+  int4 *d_conn = nullptr;
+  float4 *d_bvh = nullptr;
+  uint32_t *d_codes = nullptr;      // sorted Morton codes
+  uint32_t *d_ids = nullptr;        // sorted leaf -> cell id
+  int32_t *d_left = nullptr;        // Karras topology (n_cells - 1 inner nodes)
+  int32_t *d_right = nullptr;
+  int32_t *d_parent = nullptr;      // 2 n_cells - 1 entries, root's is -1
+  float4 *d_inner_box = nullptr;    // 2 per inner node: lo, hi
+  float bvh_build_ms = 0.f;
 };
 
 }  // namespace gvr
@@ -114,6 +134,7 @@ struct gvr_scene {
   int d_domains_cap = 0;
   float4 *d_lut = nullptr;               // LUT of the last render
   int *d_any_empty = nullptr;            // per-domain empty-brick flags
+  bool has_hex = false;
   gvr::Tuning tuning;
   unsigned long long *d_counters = nullptr;  // [0] samples
   float4 *d_rgba_tmp = nullptr;          // device image for host outputs
@@ -157,11 +178,23 @@ cudaError_t launch_empty_bricks(const float2 *brick_range, int64_t n_bricks,
                                 uint8_t *brick_empty, int *any_empty,
                                 cudaStream_t stream);
 
+// sort / scan (gvr_sort.cu)
+size_t scan_scratch_words(int64_t n);
+cudaError_t exclusive_scan(uint32_t *data, int64_t n, uint32_t *tmp, cudaStream_t stream);
+size_t sort_scratch_words(int64_t n);
+template <typename K>
+cudaError_t radix_sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *vals_tmp,
+                             int64_t n, int key_bits, uint32_t *scratch, cudaStream_t stream);
+
+// hexahedral domains (gvr_hex.cu)
+void free_hex(Domain &d);
+int hex_update_field(Domain &d, const void *field, int dtype, int64_t stride, int location);
+
 // march kernel (gvr_march.cu)
 cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          const MarchParams &mp, const float4 *d_lut,
                          float4 *d_rgba, float *d_depth,
                          unsigned long long *d_samples, const Tuning &tuning,
-                         cudaStream_t stream);
+                         bool has_hex, cudaStream_t stream);
 
 }  // namespace gvr

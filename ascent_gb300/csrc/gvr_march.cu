@@ -20,7 +20,7 @@
 // buffer or sort pass is needed.
 #include <cfloat>
 
-#include "gvr_internal.h"
+#include "gvr_hex_device.cuh"
 
 namespace gvr {
 namespace {
@@ -273,8 +273,60 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
   }
 }
 
+// Hexahedral domain: each sample is located by Newton's method in the cell
+// of the previous sample (starting from its reference coordinates), and
+// only when that fails by a walk of the LBVH; the eight corner records of
+// the current cell stay in registers between samples. Samples outside every
+// cell contribute nothing but are counted, like the structured stepping rule.
+__device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
+                         const MarchParams &mp, const float4 *lut, float thr, float4 &acc)
+{
+  float4 v[8];
+  int cur = -1;
+  float rst[3] = {0.5f, 0.5f, 0.5f};
+  int count = 0;
+  for (int k = 0;; ++k) {
+    const float t = fmaf((float)k, mp.sample_dist, t0);
+    if (!(t < t1)) break;
+    ++count;
+    const float p[3] = {fmaf(t, r.d[0], r.o[0]), fmaf(t, r.d[1], r.o[1]), fmaf(t, r.d[2], r.o[2])};
+    bool found = false;
+    if (cur >= 0) {
+      float g[3] = {rst[0], rst[1], rst[2]};
+      if (hex_newton(v, p, g)) {
+        found = true;
+        rst[0] = g[0]; rst[1] = g[1]; rst[2] = g[2];
+      }
+    }
+    if (!found) {
+      cur = hex_locate(dm, p, rst, v);
+      found = cur >= 0;
+    }
+    if (!found) continue;
+    float val;
+    if (dm.assoc == GVR_ASSOC_ELEMENT) {
+      val = __ldg(dm.cells + cur);
+    } else {
+      float n[8];
+      hex_weights(__saturatef(rst[0]), __saturatef(rst[1]), __saturatef(rst[2]), n);
+      val = 0.f;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) val = fmaf(n[i], v[i].w, val);
+    }
+    const float s = __saturatef((val - mp.scalar_min) * mp.inv_range);
+    const float4 col = lut_fetch(lut, mp.lut_size, mp.lut_filter, s);
+    const float wa = (1.f - acc.w) * col.w;
+    acc.x = fmaf(wa, col.x, acc.x);
+    acc.y = fmaf(wa, col.y, acc.y);
+    acc.z = fmaf(wa, col.z, acc.z);
+    acc.w += wa;
+    if (acc.w >= thr) break;
+  }
+  return count;
+}
+
 // PW x (32 / PW) pixel packet per warp, 16 x 16 pixels per CTA.
-template <int PW, int UNROLL, int MINB>
+template <int PW, int UNROLL, int MINB, bool HEX = false>
 __global__ void __launch_bounds__(kThreads, MINB)
 march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
              const MarchParams mp, const float4 *__restrict__ g_lut,
@@ -339,8 +391,10 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
       const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
       const DomainDev &dm = doms[best];
-      if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
-          !(mp.skip_empty && *dm.any_empty))
+      if (HEX && dm.kind == GVR_DOMAIN_HEX)
+        count += march_hex(dm, r, bt0, bt1, mp, lut, thr, acc);
+      else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
+               !(mp.skip_empty && *dm.any_empty))
         count += march_uniform<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
       else
         count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
@@ -416,8 +470,9 @@ using MarchFn = void (*)(const DomainDev *, const ViewDev, const MarchParams, co
 template <int PW, int UNROLL, int MINB>
 MarchFn pick() { return march_kernel<PW, UNROLL, MINB>; }
 
-MarchFn select(const Tuning &t)
+MarchFn select(const Tuning &t, bool has_hex)
 {
+  if (has_hex) return t.packet_w == 4 ? march_kernel<4, 1, 3, true> : march_kernel<8, 1, 3, true>;
   const int u = t.unroll >= 2 ? 2 : 1;
   const int m = t.min_blocks >= 4 ? 4 : 3;
   switch (t.packet_w) {
@@ -435,10 +490,10 @@ MarchFn select(const Tuning &t)
 cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          const MarchParams &mp, const float4 *d_lut, float4 *d_rgba,
                          float *d_depth, unsigned long long *d_samples, const Tuning &tuning,
-                         cudaStream_t stream)
+                         bool has_hex, cudaStream_t stream)
 {
   const size_t smem = sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains;
-  MarchFn fn = select(tuning);
+  MarchFn fn = select(tuning, has_hex);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(sizeof(float4) * kMaxLut + sizeof(DomainDev) * kMaxDomains));
   if (e != cudaSuccess) return e;

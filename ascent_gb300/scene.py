@@ -37,6 +37,7 @@ class Scene:
         N.call("gvr_scene_create", int(device), C.byref(h))
         self.handle = h
         self.device = int(device)
+        self._hex_cells = {}
 
     def add_uniform(self, field, origin, spacing, association: int = N.ASSOC_VERTEX) -> int:
         """field shaped (nz, ny, nx) nodes (or cells for element association)."""
@@ -63,6 +64,60 @@ class Scene:
                N.dptr(xs[2]), ptr, code, 1, int(association), loc, C.byref(did))
         del keep
         return did.value
+
+    def add_hex(self, x, y, z, conn, field, association: int = N.ASSOC_VERTEX) -> int:
+        """Unstructured hexahedra: node coordinates x, y, z (float32/float64), conn
+        (n_cells, 8) int32/int64 in VTK hexahedron order, a vertex or element field.
+        Arrays are all numpy (host) or all torch CUDA tensors (device)."""
+        cx, ctype, k1, loc, nn = _field_args(x)
+        cy, _, k2, _, _ = _field_args(y)
+        cz, _, k3, _, _ = _field_args(z)
+        fp, ftype, k4, _, _ = _field_args(field)
+        try:
+            import torch
+            is_t = isinstance(conn, torch.Tensor)
+        except ImportError:  # pragma: no cover
+            is_t = False
+        if is_t:
+            cc = conn.contiguous()
+            c64 = int(cc.dtype == torch.int64)
+            cptr, ncells = C.c_void_p(cc.data_ptr()), cc.numel() // 8
+        else:
+            cc = np.ascontiguousarray(conn)
+            if cc.dtype not in (np.int32, np.int64):
+                cc = cc.astype(np.int32)
+            c64 = int(cc.dtype == np.int64)
+            cptr, ncells = C.c_void_p(cc.ctypes.data), cc.size // 8
+        did = C.c_int(-1)
+        N.call("gvr_scene_add_hex", self.handle, int(nn), cx, cy, cz, ctype, int(ncells), cptr, c64,
+               fp, ftype, int(association), loc, C.byref(did))
+        del k1, k2, k3, k4, cc
+        self._hex_cells[did.value] = int(ncells)
+        return did.value
+
+    def hex_bvh(self, domain_id: int) -> dict:
+        """The domain's LBVH as host arrays (for checking against a CPU rebuild)."""
+        n = self.hex_cells(domain_id)
+        out = {"codes": np.zeros(n, np.uint32), "ids": np.zeros(n, np.uint32),
+               "left": np.zeros(max(n - 1, 1), np.int32), "right": np.zeros(max(n - 1, 1), np.int32),
+               "parent": np.zeros(max(2 * n - 1, 1), np.int32),
+               "inner_box": np.zeros((max(n - 1, 1), 6), np.float32)}
+        ms = C.c_float(0)
+        N.call("gvr_scene_hex_bvh", self.handle, int(domain_id), *[C.c_void_p(out[k].ctypes.data) for k in
+               ("codes", "ids", "left", "right", "parent", "inner_box")], C.byref(ms))
+        out["build_ms"] = ms.value
+        return out
+
+    def hex_cells(self, domain_id: int) -> int:
+        return int(self._hex_cells[domain_id])
+
+    def hex_locate(self, domain_id: int, points):
+        p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        cells = np.zeros(len(p), np.int32)
+        rst = np.zeros((len(p), 3), np.float32)
+        N.call("gvr_scene_hex_locate", self.handle, int(domain_id), C.c_void_p(p.ctypes.data), len(p),
+               C.c_void_p(cells.ctypes.data), C.c_void_p(rst.ctypes.data))
+        return cells, rst
 
     def update_field(self, domain_id: int, field) -> None:
         ptr, code, keep, loc, _ = _field_args(field)

@@ -114,4 +114,7 @@ def workload_params(wl, **kw) -> N.RenderParams:
 
 def load_workload(scene: S.Scene, wl) -> None:
     for d in wl.domains:
-        scene.add_uniform(d.field, d.origin, d.spacing)
+        if hasattr(d, "conn"):
+            scene.add_hex(d.x, d.y, d.z, d.conn, d.field)
+        else:
+            scene.add_uniform(d.field, d.origin, d.spacing)

@@ -61,7 +61,8 @@ class Workload:
 
     @property
     def single_domain(self) -> bool:
-        return len(self.domains) == 1
+        """One structured domain: the reference's RenderOneDomainPerRank path."""
+        return len(self.domains) == 1 and isinstance(self.domains[0], UniformDomain)
 
 
 def linear_ramp_tf(n: int = 256, alpha_max: float = 0.3):
@@ -141,6 +142,54 @@ def plain_small(n: int = 64, seed: int = 1, width: int = 512, height: int = 512,
     rp, rgb, ap, al = linear_ramp_tf()
     return Workload(f"uniform{n}^3x{len(doms)}dom@{width}x{height}", doms, width, height, samples,
                     30.0, 20.0, rp, rgb, ap, al)
+
+
+@dataclass
+class HexDomain:
+    x: np.ndarray            # node coordinates, float32
+    y: np.ndarray
+    z: np.ndarray
+    conn: np.ndarray         # (n_cells, 8) int32, VTK hexahedron order
+    field: np.ndarray        # node values, float32
+
+    @property
+    def bounds(self):
+        return np.array([self.x.min(), self.x.max(), self.y.min(), self.y.max(), self.z.min(),
+                         self.z.max()], dtype=np.float64)
+
+
+def hex_grid_connectivity(n: int) -> np.ndarray:
+    """(n^3, 8) int32 node ids of the hexahedra of an n^3-cell grid of (n+1)^3
+    nodes (x fastest), in VTK hexahedron order."""
+    m = n + 1
+    k, j, i = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    base = ((k * m + j) * m + i).astype(np.int64).ravel()
+    off = np.array([0, 1, m + 1, m, m * m, m * m + 1, m * m + m + 1, m * m + m], dtype=np.int64)
+    return (base[:, None] + off[None, :]).astype(np.int32)
+
+
+def hex_mesh(n_cells: int = 200, seed: int = 3, width: int = 1024, height: int = 1024,
+             jitter: float = 0.2) -> Workload:
+    """n_cells^3 hexahedra from a uniform grid on the unit cube with every node
+    moved by U[-jitter, jitter] cell per axis (seeded), and a float32 nodal field
+    of Gaussian blobs evaluated at the moved nodes; samples ~ 0.5 cell."""
+    rng = np.random.default_rng(seed)
+    m = n_cells + 1
+    h = 1.0 / n_cells
+    g = np.arange(m, dtype=np.float64) * h
+    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    pts = [c.ravel() + rng.uniform(-jitter * h, jitter * h, size=m ** 3) for c in (x, y, z)]
+    c, s, a = blob_params(rng)
+    f = np.zeros(m ** 3, dtype=np.float64)
+    for cc, ss, aa in zip(c, s, a):
+        d2 = (pts[0] - cc[0]) ** 2 + (pts[1] - cc[1]) ** 2 + (pts[2] - cc[2]) ** 2
+        f += aa * np.exp(-d2 / (2 * ss * ss))
+    dom = HexDomain(*(p.astype(np.float32) for p in pts), hex_grid_connectivity(n_cells),
+                    f.astype(np.float32))
+    samples = int(np.ceil(np.sqrt(3.0) * n_cells / 0.5))
+    rp, rgb, ap, al = linear_ramp_tf()
+    return Workload(f"hex{n_cells}^3@{width}x{height}", [dom], width, height, samples, 30.0, 20.0,
+                    rp, rgb, ap, al)
 
 
 def plain_large(n_cells: int = 512, seed: int = 2, width: int = 1024, height: int = 1024,

@@ -199,6 +199,37 @@ GVR_API int gvr_scene_add_rectilinear(gvr_scene *scene, const int dims[3],
                               const void *field, int dtype, int64_t stride,
                               int association, int location, int *domain_id);
 
+/* Add an unstructured hexahedral domain: n_nodes node coordinates in three
+ * arrays x, y, z (float32 or float64, Blueprint explicit coordset), n_cells
+ * cells of 8 node ids each in VTK hexahedron order (int32, or int64 when
+ * conn_int64), and a scalar field per node (vertex) or per cell (element).
+ * All arrays are in `location` memory. The domain's LBVH (Morton codes,
+ * Karras radix tree, box refit) is built on the device. Replaces the
+ * unstructured path of the Blueprint adapter
+ * (ascent_vtkh_data_adapter.cpp:1618-1780) and the ConnectivityProxy set-up
+ * of VolumeRenderer's UnstructuredWrapper (VolumeRenderer.cpp:182-220). */
+GVR_API int gvr_scene_add_hex(gvr_scene *scene, int64_t n_nodes, const void *x,
+                              const void *y, const void *z, int coord_dtype,
+                              int64_t n_cells, const void *conn, int conn_int64,
+                              const void *field, int dtype, int association,
+                              int location, int *domain_id);
+
+/* Copy a hex domain's LBVH to host arrays (any may be NULL): sorted Morton
+ * codes and leaf cell ids (n_cells each), Karras children left/right
+ * (n_cells-1; values >= n_cells-1 are leaves n - (n_cells-1)), parents
+ * (2 n_cells - 1, root -1), inner boxes (6 floats lo xyz, hi xyz per inner
+ * node) and the build's wall time in ms. For checking the build against a
+ * CPU rebuild (Devil Ray's LinearBVHBuilder, linear_bvh_builder.cpp:60-520). */
+GVR_API int gvr_scene_hex_bvh(const gvr_scene *scene, int domain_id, uint32_t *codes,
+                              uint32_t *ids, int32_t *left, int32_t *right,
+                              int32_t *parent, float *inner_boxes, float *build_ms);
+
+/* Locate n points (3 n host floats) in a hex domain: cells[i] = containing
+ * cell or -1, rst = reference coordinates (Devil Ray's DeviceMesh::locate,
+ * data_model/device_mesh.hpp:250-360, with NewtonSolve). */
+GVR_API int gvr_scene_hex_locate(gvr_scene *scene, int domain_id, const float *points,
+                                 int n, int *cells, float *rst);
+
 /* Replace the field of an existing domain (same size, type rules as the
  * add call); the bricked copy and macrocell ranges are rebuilt on device. */
 GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *field,

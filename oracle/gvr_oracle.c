@@ -379,6 +379,14 @@ typedef struct {
   REAL lo[3], hi[3];  /* bounds */
   const float *field; /* caller-owned */
   int assoc;
+  /* hexahedral domains */
+  int64_t n_nodes, n_cells;
+  const float *hx, *hy, *hz; /* caller-owned node coordinates */
+  const int *conn;           /* caller-owned, 8 per cell */
+  float *leaf_lo, *leaf_hi;  /* 3 per cell */
+  uint32_t *codes, *ids;     /* sorted Morton codes, leaf -> cell */
+  int *left, *right, *parent;
+  float *inner_box;          /* 6 per inner node */
 } or_domain;
 
 typedef struct {
@@ -395,8 +403,12 @@ or_scene *or_scene_new(void)
 void or_scene_free(or_scene *s)
 {
   if (!s) return;
-  for (int i = 0; i < s->n; ++i)
-    for (int a = 0; a < 3; ++a) free(s->d[i].coord[a]);
+  for (int i = 0; i < s->n; ++i) {
+    or_domain *d = &s->d[i];
+    for (int a = 0; a < 3; ++a) free(d->coord[a]);
+    free(d->leaf_lo); free(d->leaf_hi); free(d->codes); free(d->ids);
+    free(d->left); free(d->right); free(d->parent); free(d->inner_box);
+  }
   free(s->d);
   free(s);
 }
@@ -446,6 +458,322 @@ int or_scene_add_rectilinear(or_scene *s, const int dims[3], const double *x,
   d->field = field;
   d->assoc = assoc;
   return s->n - 1;
+}
+
+
+/* ------------------------------------------------------------------ */
+/* Hexahedral domains: CPU rebuild of the LBVH (Devil Ray's             */
+/* LinearBVHBuilder, src/libs/dray/linear_bvh_builder.cpp:60-520) and   */
+/* point location (DeviceMesh::locate, data_model/device_mesh.hpp:      */
+/* 250-360, NewtonSolve, newton_solver.hpp:33-110).                     */
+/* The box, centre and Morton arithmetic is float32 with every rounding */
+/* step explicit (this file is built with -ffp-contract=off), so codes, */
+/* order and topology match the device build bit for bit. Equal codes   */
+/* are ordered by cell id (the reference's std::sort leaves that order  */
+/* unspecified).                                                        */
+/* ------------------------------------------------------------------ */
+static uint32_t spread3(uint32_t x)
+{
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+static uint32_t quant10(float u)
+{
+  float q = u * 1024.0f;
+  q = q < 0.0f ? 0.0f : q;
+  q = q > 1023.0f ? 1023.0f : q;
+  return (uint32_t)q;
+}
+
+static const uint32_t *g_sort_codes;
+static int cmp_code(const void *a, const void *b)
+{
+  uint32_t ia = *(const uint32_t *)a, ib = *(const uint32_t *)b;
+  uint32_t ca = g_sort_codes[ia], cb = g_sort_codes[ib];
+  if (ca != cb) return ca < cb ? -1 : 1;
+  return ia < ib ? -1 : (ia > ib ? 1 : 0);
+}
+
+static int prefix_len(const uint32_t *codes, int n, int a, int b)
+{
+  if (b < 0 || b >= n) return -1;
+  uint32_t x = codes[a] ^ codes[b];
+  if (x) return __builtin_clz(x);
+  return 32 + __builtin_clz((uint32_t)a ^ (uint32_t)b);
+}
+
+static void hex_build(or_domain *d)
+{
+  const int64_t nc = d->n_cells;
+  d->leaf_lo = (float *)malloc(sizeof(float) * 3 * nc);
+  d->leaf_hi = (float *)malloc(sizeof(float) * 3 * nc);
+  float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
+  const float *xyz[3] = {d->hx, d->hy, d->hz};
+  for (int64_t c = 0; c < nc; ++c) {
+    for (int a = 0; a < 3; ++a) {
+      float l = INFINITY, h = -INFINITY;
+      for (int k = 0; k < 8; ++k) {
+        float v = xyz[a][d->conn[8 * c + k]];
+        l = v < l ? v : l;
+        h = v > h ? v : h;
+      }
+      d->leaf_lo[3 * c + a] = l;
+      d->leaf_hi[3 * c + a] = h;
+      bl[a] = l < bl[a] ? l : bl[a];
+      bh[a] = h > bh[a] ? h : bh[a];
+    }
+  }
+  float inv[3];
+  for (int a = 0; a < 3; ++a) {
+    float ext = bh[a] - bl[a];
+    inv[a] = ext == 0.0f ? 0.0f : 1.0f / ext;
+    d->lo[a] = bl[a];
+    d->hi[a] = bh[a];
+  }
+  uint32_t *codes = (uint32_t *)malloc(sizeof(uint32_t) * nc);
+  for (int64_t c = 0; c < nc; ++c) {
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+      float cen = 0.5f * (d->leaf_lo[3 * c + a] + d->leaf_hi[3 * c + a]);
+      float u = (cen - bl[a]) * inv[a];
+      q[a] = quant10(u);
+    }
+    codes[c] = (spread3(q[2]) << 2) | (spread3(q[1]) << 1) | spread3(q[0]);
+  }
+  d->ids = (uint32_t *)malloc(sizeof(uint32_t) * nc);
+  for (int64_t c = 0; c < nc; ++c) d->ids[c] = (uint32_t)c;
+  g_sort_codes = codes;
+  qsort(d->ids, nc, sizeof(uint32_t), cmp_code);
+  d->codes = (uint32_t *)malloc(sizeof(uint32_t) * nc);
+  for (int64_t k = 0; k < nc; ++k) d->codes[k] = codes[d->ids[k]];
+  free(codes);
+  if (nc < 2) return;
+  const int n = (int)nc, ni = n - 1;
+  d->left = (int *)malloc(sizeof(int) * ni);
+  d->right = (int *)malloc(sizeof(int) * ni);
+  d->parent = (int *)malloc(sizeof(int) * (2 * n - 1));
+  d->inner_box = (float *)malloc(sizeof(float) * 6 * ni);
+  const uint32_t *k = d->codes;
+  /* Karras 2012, "Maximizing parallelism in the construction of BVHs,
+   * octrees, and k-d trees", Figure 4 */
+  for (int i = 0; i < ni; ++i) {
+    int dd = prefix_len(k, n, i, i + 1) - prefix_len(k, n, i, i - 1) < 0 ? -1 : 1;
+    int dmin = prefix_len(k, n, i, i - dd);
+    int lmax = 2;
+    while (prefix_len(k, n, i, i + lmax * dd) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+      if (prefix_len(k, n, i, i + (l + t) * dd) > dmin) l += t;
+    int j = i + l * dd;
+    int dnode = prefix_len(k, n, i, j);
+    int sidx = 0;
+    for (int e = 1;; ++e) {
+      int t = (l + (1 << e) - 1) >> e;
+      if (prefix_len(k, n, i, i + (sidx + t) * dd) > dnode) sidx += t;
+      if (t <= 1) break;
+    }
+    int split = i + sidx * dd + (dd < 0 ? dd : 0);
+    int lo = i < j ? i : j, hi = i < j ? j : i;
+    int lc = lo == split ? ni + split : split;
+    int rc = hi == split + 1 ? ni + split + 1 : split + 1;
+    d->left[i] = lc;
+    d->right[i] = rc;
+    d->parent[lc] = i;
+    d->parent[rc] = i;
+  }
+  d->parent[0] = -1;
+  /* boxes of inner nodes, children before parents: post-order by explicit stack */
+  int *stack = (int *)malloc(sizeof(int) * 2 * n);
+  char *done = (char *)calloc(ni, 1);
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    int node = stack[sp - 1];
+    int ch[2] = {d->left[node], d->right[node]};
+    int pushed = 0;
+    for (int q = 0; q < 2; ++q)
+      if (ch[q] < ni && !done[ch[q]]) { stack[sp++] = ch[q]; pushed = 1; }
+    if (pushed) continue;
+    --sp;
+    float *b = d->inner_box + 6 * node;
+    for (int a = 0; a < 3; ++a) { b[a] = INFINITY; b[3 + a] = -INFINITY; }
+    for (int q = 0; q < 2; ++q) {
+      const float *cl, *chh;
+      if (ch[q] >= ni) {
+        uint32_t cell = d->ids[ch[q] - ni];
+        cl = d->leaf_lo + 3 * cell;
+        chh = d->leaf_hi + 3 * cell;
+      } else {
+        cl = d->inner_box + 6 * ch[q];
+        chh = cl + 3;
+      }
+      for (int a = 0; a < 3; ++a) {
+        b[a] = cl[a] < b[a] ? cl[a] : b[a];
+        b[3 + a] = chh[a] > b[3 + a] ? chh[a] : b[3 + a];
+      }
+    }
+    done[node] = 1;
+  }
+  free(stack);
+  free(done);
+}
+
+int or_scene_add_hex(or_scene *s, int64_t n_nodes, const float *x, const float *y,
+                     const float *z, int64_t n_cells, const int *conn, const float *field,
+                     int assoc)
+{
+  if (n_cells < 1 || n_nodes < 8) return -1;
+  or_domain *d = push(s);
+  d->kind = GVR_DOMAIN_HEX;
+  d->n_nodes = n_nodes;
+  d->n_cells = n_cells;
+  d->hx = x; d->hy = y; d->hz = z;
+  d->conn = conn;
+  d->field = field;
+  d->assoc = assoc;
+  hex_build(d);
+  return s->n - 1;
+}
+
+/* Copy the LBVH of a hex domain (same layout as gvr_scene_hex_bvh). */
+int or_hex_bvh(const or_scene *s, int dom, uint32_t *codes, uint32_t *ids, int *left,
+               int *right, int *parent, float *inner_box)
+{
+  const or_domain *d = &s->d[dom];
+  const int64_t nc = d->n_cells;
+  memcpy(codes, d->codes, sizeof(uint32_t) * nc);
+  memcpy(ids, d->ids, sizeof(uint32_t) * nc);
+  if (nc > 1) {
+    memcpy(left, d->left, sizeof(int) * (nc - 1));
+    memcpy(right, d->right, sizeof(int) * (nc - 1));
+    memcpy(parent, d->parent, sizeof(int) * (2 * nc - 1));
+    memcpy(inner_box, d->inner_box, sizeof(float) * 6 * (nc - 1));
+  }
+  return GVR_OK;
+}
+
+/* Newton's method on the trilinear map of cell c (VTK hex order). */
+static int hex_newton(const or_domain *d, int64_t c, const REAL p[3], REAL rst[3])
+{
+  REAL X[8][3];
+  for (int i = 0; i < 8; ++i) {
+    int nid = d->conn[8 * c + i];
+    X[i][0] = d->hx[nid]; X[i][1] = d->hy[nid]; X[i][2] = d->hz[nid];
+  }
+  const REAL tol = sizeof(REAL) == 8 ? (REAL)1e-10 : (REAL)1e-5;
+  const REAL in_tol = (REAL)1e-4;
+  REAL r = rst[0], sv = rst[1], t = rst[2];
+  int conv = 0;
+  for (int it = 0; it < 10; ++it) {
+    REAL r0 = 1 - r, s0 = 1 - sv, t0 = 1 - t;
+    REAL n[8] = {r0 * s0 * t0, r * s0 * t0, r * sv * t0, r0 * sv * t0,
+                 r0 * s0 * t, r * s0 * t, r * sv * t, r0 * sv * t};
+    REAL dr[8] = {-s0 * t0, s0 * t0, sv * t0, -sv * t0, -s0 * t, s0 * t, sv * t, -sv * t};
+    REAL ds[8] = {-r0 * t0, -r * t0, r * t0, r0 * t0, -r0 * t, -r * t, r * t, r0 * t};
+    REAL dt[8] = {-r0 * s0, -r * s0, -r * sv, -r0 * sv, r0 * s0, r * s0, r * sv, r0 * sv};
+    REAL F[3] = {-p[0], -p[1], -p[2]}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int i = 0; i < 8; ++i)
+      for (int a = 0; a < 3; ++a) {
+        F[a] += n[i] * X[i][a];
+        J[a][0] += dr[i] * X[i][a];
+        J[a][1] += ds[i] * X[i][a];
+        J[a][2] += dt[i] * X[i][a];
+      }
+    REAL c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    REAL c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    REAL c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    REAL det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    if (!(det > 0 || det < 0)) return 0;
+    REAL c10 = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    REAL c11 = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    REAL c12 = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    REAL c20 = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    REAL c21 = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    REAL c22 = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    REAL d0 = (c00 * F[0] + c10 * F[1] + c20 * F[2]) / det;
+    REAL d1 = (c01 * F[0] + c11 * F[1] + c21 * F[2]) / det;
+    REAL d2 = (c02 * F[0] + c12 * F[1] + c22 * F[2]) / det;
+    r -= d0; sv -= d1; t -= d2;
+    if (!(fabs((double)r) < 1e3 && fabs((double)sv) < 1e3 && fabs((double)t) < 1e3)) return 0;
+    REAL m = fabs((double)d0);
+    if (fabs((double)d1) > m) m = fabs((double)d1);
+    if (fabs((double)d2) > m) m = fabs((double)d2);
+    if (m < tol) { conv = 1; break; }
+  }
+  rst[0] = r; rst[1] = sv; rst[2] = t;
+  return conv && r >= -in_tol && r <= 1 + in_tol && sv >= -in_tol && sv <= 1 + in_tol &&
+         t >= -in_tol && t <= 1 + in_tol;
+}
+
+static int in_box(const REAL p[3], const float *lo, const float *hi)
+{
+  return !(p[0] < lo[0] || p[1] < lo[1] || p[2] < lo[2] || p[0] > hi[0] || p[1] > hi[1] ||
+           p[2] > hi[2]);
+}
+
+/* First cell containing p in left-first traversal order, or -1. */
+static int64_t hex_locate(const or_domain *d, const REAL p[3], REAL rst[3])
+{
+  const int64_t nc = d->n_cells;
+  if (nc == 1) {
+    rst[0] = rst[1] = rst[2] = (REAL)0.5;
+    return hex_newton(d, 0, p, rst) ? 0 : -1;
+  }
+  const int ni = (int)nc - 1;
+  int stack[128];
+  int sp = 0, node = 0; /* node < ni: inner, else leaf node - ni */
+  for (;;) {
+    if (node < ni) {
+      int ch[2] = {d->left[node], d->right[node]};
+      int in[2];
+      for (int q = 0; q < 2; ++q) {
+        const float *lo, *hi;
+        if (ch[q] >= ni) {
+          uint32_t cell = d->ids[ch[q] - ni];
+          lo = d->leaf_lo + 3 * cell;
+          hi = d->leaf_hi + 3 * cell;
+        } else {
+          lo = d->inner_box + 6 * ch[q];
+          hi = lo + 3;
+        }
+        in[q] = in_box(p, lo, hi);
+      }
+      if (!in[0] && !in[1]) {
+        if (!sp) return -1;
+        node = stack[--sp];
+        continue;
+      }
+      if (in[0] && in[1]) {
+        if (sp < 128) stack[sp++] = ch[1];
+        node = ch[0];
+      } else {
+        node = in[0] ? ch[0] : ch[1];
+      }
+    } else {
+      int64_t cell = d->ids[node - ni];
+      rst[0] = rst[1] = rst[2] = (REAL)0.5;
+      if (hex_newton(d, cell, p, rst)) return cell;
+      if (!sp) return -1;
+      node = stack[--sp];
+    }
+  }
+}
+
+int or_hex_locate(const or_scene *s, int dom, const float *pts, int n, int *cells, float *rst)
+{
+  const or_domain *d = &s->d[dom];
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < n; ++i) {
+    REAL p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]}, r[3];
+    cells[i] = (int)hex_locate(d, p, r);
+    for (int a = 0; a < 3; ++a) rst[3 * i + a] = (float)r[a];
+  }
+  return GVR_OK;
 }
 
 /* ------------------------------------------------------------------ */
@@ -502,8 +830,22 @@ static void locate_axis(const or_domain *d, int a, REAL p, int *i, REAL *w)
   }
 }
 
-static REAL sample_field(const or_domain *d, v3 p)
+static REAL sample_field(const or_domain *d, v3 p, int *found)
 {
+  *found = 1;
+  if (d->kind == GVR_DOMAIN_HEX) {
+    REAL q[3] = {p.x, p.y, p.z}, rst[3];
+    int64_t c = hex_locate(d, q, rst);
+    if (c < 0) { *found = 0; return 0; }
+    if (d->assoc == GVR_ASSOC_ELEMENT) return (REAL)d->field[c];
+    for (int a = 0; a < 3; ++a) rst[a] = rst[a] < 0 ? 0 : (rst[a] > 1 ? 1 : rst[a]);
+    REAL r = rst[0], sv = rst[1], t = rst[2], r0 = 1 - r, s0 = 1 - sv, t0 = 1 - t;
+    REAL n[8] = {r0 * s0 * t0, r * s0 * t0, r * sv * t0, r0 * sv * t0,
+                 r0 * s0 * t, r * s0 * t, r * sv * t, r0 * sv * t};
+    REAL v = 0;
+    for (int i = 0; i < 8; ++i) v += n[i] * (REAL)d->field[d->conn[8 * c + i]];
+    return v;
+  }
   int i[3];
   REAL w[3];
   REAL pp[3] = {p.x, p.y, p.z};
@@ -560,7 +902,9 @@ static int64_t march(const or_domain *d, v3 o, v3 dir, REAL t0, REAL t1,
     if (!(t < t1)) break;
     ++count;
     v3 pos = add(o, scl(dir, t));
-    REAL v = sample_field(d, pos);
+    int found;
+    REAL v = sample_field(d, pos, &found);
+    if (!found) continue;
     REAL s = (v - smin) * inv_range;
     if (s < 0) s = 0;
     if (s > 1) s = 1;

@@ -64,6 +64,9 @@ def load(precision: int = 64) -> C.CDLL:
     lib.or_scene_free.argtypes = [vp]
     lib.or_scene_add_uniform.argtypes = [vp, P(i), P(d), P(d), P(f), i]
     lib.or_scene_add_rectilinear.argtypes = [vp, P(i), P(d), P(d), P(d), P(f), i]
+    lib.or_scene_add_hex.argtypes = [vp, C.c_int64, P(f), P(f), P(f), C.c_int64, P(i), P(f), i]
+    lib.or_hex_bvh.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
+    lib.or_hex_locate.argtypes = [vp, i, P(f), i, P(i), P(f)]
     lib.or_render.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
     lib.or_render_rows.argtypes = [vp, P(Camera), P(RenderParams), i, i, P(f), P(f), P(C.c_uint64)]
     lib.or_num_threads.restype = i
@@ -110,6 +113,36 @@ class OracleScene:
         self._keep += [dims_a, f, *xs]
         return self.lib.or_scene_add_rectilinear(self.handle, dims_p, dptr(xs[0]), dptr(xs[1]),
                                                  dptr(xs[2]), fptr(f), int(assoc))
+
+    def add_hex(self, x, y, z, conn, field, assoc=0) -> int:
+        xs = [np.ascontiguousarray(c, dtype=np.float32) for c in (x, y, z)]
+        cn = np.ascontiguousarray(conn, dtype=np.int32).ravel()
+        f = np.ascontiguousarray(field, dtype=np.float32).ravel()
+        self._keep += [*xs, cn, f]
+        self._ncells = getattr(self, "_ncells", {})
+        did = self.lib.or_scene_add_hex(self.handle, len(xs[0]), fptr(xs[0]), fptr(xs[1]), fptr(xs[2]),
+                                        len(cn) // 8, cn.ctypes.data_as(C.POINTER(C.c_int)), fptr(f),
+                                        int(assoc))
+        self._ncells[did] = len(cn) // 8
+        return did
+
+    def hex_bvh(self, dom: int) -> dict:
+        n = self._ncells[dom]
+        out = {"codes": np.zeros(n, np.uint32), "ids": np.zeros(n, np.uint32),
+               "left": np.zeros(max(n - 1, 1), np.int32), "right": np.zeros(max(n - 1, 1), np.int32),
+               "parent": np.zeros(max(2 * n - 1, 1), np.int32),
+               "inner_box": np.zeros((max(n - 1, 1), 6), np.float32)}
+        self.lib.or_hex_bvh(self.handle, dom, *[out[k].ctypes.data for k in
+                            ("codes", "ids", "left", "right", "parent", "inner_box")])
+        return out
+
+    def hex_locate(self, dom: int, points):
+        p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        cells = np.zeros(len(p), np.int32)
+        rst = np.zeros((len(p), 3), np.float32)
+        self.lib.or_hex_locate(self.handle, dom, fptr(p), len(p), cells.ctypes.data_as(C.POINTER(C.c_int)),
+                               fptr(rst))
+        return cells, rst
 
     def render(self, cam: Camera, params: RenderParams):
         w, h = params.width, params.height
