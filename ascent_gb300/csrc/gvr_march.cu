@@ -472,7 +472,8 @@ MarchFn pick() { return march_kernel<PW, UNROLL, MINB>; }
 
 MarchFn select(const Tuning &t, bool has_hex)
 {
-  if (has_hex) return t.packet_w == 4 ? march_kernel<4, 1, 3, true> : march_kernel<8, 1, 3, true>;
+  // the hex path keeps eight corner records in registers: 2 CTAs per SM
+  if (has_hex) return t.packet_w == 4 ? march_kernel<4, 1, 2, true> : march_kernel<8, 1, 2, true>;
   const int u = t.unroll >= 2 ? 2 : 1;
   const int m = t.min_blocks >= 4 ? 4 : 3;
   switch (t.packet_w) {
