@@ -130,6 +130,11 @@ _SIGS = {
     "gvr_scene_update_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int64, C.c_int]),
     "gvr_scene_num_domains": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "gvr_scene_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "gvr_scene_set_batch_granularity": (C.c_int, [C.c_void_p, C.c_int]),
+    "gvr_scene_batch_graph_builds": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "gvr_render_volume_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(RenderParams),
+                                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                          C.POINTER(C.c_uint64)]),
     "gvr_scene_bounds": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "gvr_scene_range": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gvr_render_volume": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams), C.c_void_p,

@@ -355,6 +355,13 @@ int gvr_scene_destroy(gvr_scene *s)
   cudaFree(s->d_counters);
   cudaFree(s->d_rgba_tmp);
   cudaFree(s->d_depth_tmp);
+  cudaFree(s->d_views);
+  cudaFree(s->d_rects);
+  cudaFree(s->d_queue);
+  cudaFree(s->d_batch_rgba);
+  cudaFree(s->d_batch_depth);
+  if (s->batch_exec) cudaGraphExecDestroy(s->batch_exec);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
   return GVR_OK;
 }
@@ -506,6 +513,15 @@ int gvr_scene_update_field(gvr_scene *s, int domain_id, const void *field, int d
   return upload_field(s, s->domains[domain_id], field, dtype, stride, location);
 }
 
+int gvr_scene_set_batch_granularity(gvr_scene *s, int tiles_per_item)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (tiles_per_item < 1 || tiles_per_item > 64)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "tiles_per_item must be in [1, 64]");
+  s->tuning.tiles_per_item = tiles_per_item;
+  return GVR_OK;
+}
+
 int gvr_scene_set_tuning(gvr_scene *s, int packet_w, int unroll, int min_blocks)
 {
   if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
@@ -631,26 +647,12 @@ static int ensure_buffers(gvr_scene *s, int64_t pixels, int lut_size)
   return GVR_OK;
 }
 
-int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
-                      float *rgba, float *depth, int out_location, void *stream,
-                      uint64_t *samples_out)
+// MarchParams of one render, plus the empty-brick classification of every
+// vertex-field domain against this transfer function, reused while the LUT,
+// its filter, the range and the fields stay those of the last render.
+static int prepare_march(gvr_scene *s, const gvr_render_params *p, cudaStream_t st, MarchParams &mp)
 {
-  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
-  int rc = check_camera(camera);
-  if (rc != GVR_OK) return rc;
-  if ((rc = check_params(p)) != GVR_OK) return rc;
-  if (!rgba || !depth) return set_error(GVR_ERR_INVALID_ARGUMENT, "output buffers are NULL");
-  if (out_location != GVR_MEM_HOST && out_location != GVR_MEM_DEVICE)
-    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad out_location");
-  if (s->domains.empty()) return set_error(GVR_ERR_NOT_FOUND, "scene has no domains");
-  cudaError_t e = cudaSetDevice(s->device);
-  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-  cudaStream_t st = (cudaStream_t)stream;
-  const int64_t pixels = (int64_t)p->width * p->height;
-  if ((rc = ensure_buffers(s, out_location == GVR_MEM_HOST ? pixels : 0, p->lut_size)) != GVR_OK)
-    return rc;
-
-  MarchParams mp;
+  cudaError_t e;
   std::memset(&mp, 0, sizeof(mp));
   mp.width = p->width;
   mp.height = p->height;
@@ -692,6 +694,30 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
     s->classify_inv_range = mp.inv_range;
     s->classify_valid = true;
   }
+  return GVR_OK;
+}
+
+int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
+                      float *rgba, float *depth, int out_location, void *stream,
+                      uint64_t *samples_out)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  int rc = check_camera(camera);
+  if (rc != GVR_OK) return rc;
+  if ((rc = check_params(p)) != GVR_OK) return rc;
+  if (!rgba || !depth) return set_error(GVR_ERR_INVALID_ARGUMENT, "output buffers are NULL");
+  if (out_location != GVR_MEM_HOST && out_location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad out_location");
+  if (s->domains.empty()) return set_error(GVR_ERR_NOT_FOUND, "scene has no domains");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t pixels = (int64_t)p->width * p->height;
+  if ((rc = ensure_buffers(s, out_location == GVR_MEM_HOST ? pixels : 0, p->lut_size)) != GVR_OK)
+    return rc;
+
+  MarchParams mp;
+  if ((rc = prepare_march(s, p, st, mp)) != GVR_OK) return rc;
   if (samples_out) {
     e = cudaMemsetAsync(s->d_counters, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_error(e, "clear counters");
@@ -719,6 +745,180 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "render");
   }
+  return GVR_OK;
+}
+
+
+// Conservative pixel rectangle {x0, y0, x1, y1} (inclusive) of a box seen by a
+// view: the projections of its 8 corners through the same pinhole model the
+// rays use, widened by one pixel; the whole image when a corner is not in
+// front of the camera.
+static int4 screen_rect(const ViewDev &v, const double b[6], int W, int H)
+{
+  double lo_x = 1e30, lo_y = 1e30, hi_x = -1e30, hi_y = -1e30;
+  for (int k = 0; k < 8; ++k) {
+    const double P[3] = {b[(k & 1) ? 1 : 0], b[(k & 2) ? 3 : 2], b[(k & 4) ? 5 : 4]};
+    double d[3];
+    for (int a = 0; a < 3; ++a) d[a] = P[a] - v.origin[a];
+    const double z = d[0] * v.look[0] + d[1] * v.look[1] + d[2] * v.look[2];
+    if (!(z > 1e-6)) return make_int4(0, 0, W - 1, H - 1);
+    const double a = d[0] * v.ru[0] + d[1] * v.ru[1] + d[2] * v.ru[2];
+    const double c = d[0] * v.rv[0] + d[1] * v.rv[1] + d[2] * v.rv[2];
+    const double x = a / (z * v.dx_scale) + 0.5 * W + v.xoff;
+    const double y = c / (z * v.dy_scale) + 0.5 * H + v.yoff;
+    lo_x = std::min(lo_x, x); hi_x = std::max(hi_x, x);
+    lo_y = std::min(lo_y, y); hi_y = std::max(hi_y, y);
+  }
+  const double cx0 = std::floor(lo_x) - 1, cy0 = std::floor(lo_y) - 1;
+  const double cx1 = std::ceil(hi_x) + 1, cy1 = std::ceil(hi_y) + 1;
+  if (cx1 < 0 || cy1 < 0 || cx0 > W - 1 || cy0 > H - 1) return make_int4(1, 1, 0, 0);  // empty
+  return make_int4((int)std::max(0.0, cx0), (int)std::max(0.0, cy0), (int)std::min<double>(W - 1, cx1),
+                   (int)std::min<double>(H - 1, cy1));
+}
+
+int gvr_render_volume_batch(gvr_scene *s, const gvr_camera *cameras, int n_views,
+                            const gvr_render_params *p, float *rgba, float *depth,
+                            int out_location, void *stream, uint64_t *samples_out)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (n_views < 1 || !cameras) return set_error(GVR_ERR_INVALID_ARGUMENT, "need >= 1 camera");
+  int rc;
+  for (int i = 0; i < n_views; ++i)
+    if ((rc = check_camera(cameras + i)) != GVR_OK) return rc;
+  if ((rc = check_params(p)) != GVR_OK) return rc;
+  if (!rgba || !depth) return set_error(GVR_ERR_INVALID_ARGUMENT, "output buffers are NULL");
+  if (out_location != GVR_MEM_HOST && out_location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad out_location");
+  if (s->domains.empty()) return set_error(GVR_ERR_NOT_FOUND, "scene has no domains");
+  const int64_t pixels = (int64_t)p->width * p->height;
+  if (pixels * n_views > (1ll << 30))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "views x pixels must be <= 2^30");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  if ((rc = ensure_buffers(s, 0, p->lut_size)) != GVR_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!st) {
+    if (!s->own_stream) {
+      e = cudaStreamCreate(&s->own_stream);  // blocking: ordered with the legacy stream
+      if (e != cudaSuccess) return cuda_error(e, "cudaStreamCreate");
+    }
+    st = s->own_stream;
+  }
+  const int nd = (int)s->domains.size();
+  if (n_views > s->views_cap) {
+    cudaFree(s->d_views);
+    s->d_views = nullptr;
+    s->views_cap = 0;
+    if ((e = cudaMalloc(&s->d_views, sizeof(ViewDev) * n_views)) != cudaSuccess)
+      return cuda_error(e, "cudaMalloc views");
+    s->views_cap = n_views;
+  }
+  if (n_views * nd > s->rects_cap) {
+    cudaFree(s->d_rects);
+    s->d_rects = nullptr;
+    s->rects_cap = 0;
+    if ((e = cudaMalloc(&s->d_rects, sizeof(int4) * n_views * nd)) != cudaSuccess)
+      return cuda_error(e, "cudaMalloc rects");
+    s->rects_cap = n_views * nd;
+  }
+  if (!s->d_queue && (e = cudaMalloc(&s->d_queue, 256)) != cudaSuccess)
+    return cuda_error(e, "cudaMalloc queue");
+  if (out_location == GVR_MEM_HOST && pixels * n_views > s->batch_pixels) {
+    cudaFree(s->d_batch_rgba);
+    cudaFree(s->d_batch_depth);
+    s->d_batch_rgba = nullptr;
+    s->d_batch_depth = nullptr;
+    s->batch_pixels = 0;
+    e = cudaMalloc(&s->d_batch_rgba, sizeof(float4) * pixels * n_views);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_batch_depth, sizeof(float) * pixels * n_views);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMalloc batch images");
+    s->batch_pixels = pixels * n_views;
+  }
+  MarchParams mp;
+  if ((rc = prepare_march(s, p, st, mp)) != GVR_OK) return rc;
+  std::vector<ViewDev> views(n_views);
+  std::vector<int4> rects((size_t)n_views * nd);
+  for (int v = 0; v < n_views; ++v) {
+    make_view(cameras[v], p->width, p->height, &views[v]);
+    for (int d = 0; d < nd; ++d)
+      rects[(size_t)v * nd + d] = screen_rect(views[v], s->domains[d].bounds, p->width, p->height);
+  }
+  e = cudaMemcpyAsync(s->d_views, views.data(), sizeof(ViewDev) * n_views, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->d_rects, rects.data(), sizeof(int4) * rects.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && samples_out) e = cudaMemsetAsync(s->d_counters, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return cuda_error(e, "batch set-up copies");
+  float4 *d_rgba = out_location == GVR_MEM_DEVICE ? (float4 *)rgba : s->d_batch_rgba;
+  float *d_depth = out_location == GVR_MEM_DEVICE ? depth : s->d_batch_depth;
+  unsigned long long *d_samples = samples_out ? s->d_counters : nullptr;
+
+  // The memset of the work counter and the persistent launch are captured
+  // once per launch configuration and replayed as a CUDA graph.
+  struct Key {
+    MarchParams mp;
+    int n_views, packet_w, unroll, min_blocks, tpi, has_hex;
+    const void *ptrs[6];
+  } key;
+  std::memset(&key, 0, sizeof(key));
+  key.mp = mp;
+  key.n_views = n_views;
+  key.packet_w = s->tuning.packet_w;
+  key.unroll = s->tuning.unroll;
+  key.min_blocks = s->tuning.min_blocks;
+  key.tpi = s->tuning.tiles_per_item;
+  key.has_hex = s->has_hex ? 1 : 0;
+  const void *ptrs[6] = {d_rgba, d_depth, d_samples, s->d_views, s->d_rects, s->d_domains};
+  std::memcpy(key.ptrs, ptrs, sizeof(ptrs));
+  const unsigned char *kb = reinterpret_cast<const unsigned char *>(&key);
+  if (!s->batch_exec || s->batch_key.size() != sizeof(key) ||
+      std::memcmp(s->batch_key.data(), kb, sizeof(key)) != 0) {
+    if (s->batch_exec) {
+      cudaGraphExecDestroy(s->batch_exec);
+      s->batch_exec = nullptr;
+    }
+    int grid = 0;
+    if ((e = batch_grid(mp, n_views, s->tuning, s->has_hex, &grid)) != cudaSuccess)
+      return cuda_error(e, "batch launch shape");
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamBeginCapture");
+    cudaError_t le = launch_batch(s->d_domains, s->d_views, s->d_rects, mp, n_views, s->d_lut, d_rgba,
+                                  d_depth, d_samples, s->d_queue, s->tuning, s->has_hex, grid, st);
+    e = cudaStreamEndCapture(st, &graph);
+    if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(le, "batch capture"); }
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&s->batch_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { s->batch_exec = nullptr; return cuda_error(e, "cudaGraphInstantiate"); }
+    s->batch_key.assign(kb, kb + sizeof(key));
+    ++s->batch_graph_builds;
+  }
+  e = cudaGraphLaunch(s->batch_exec, st);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
+  count_launch();
+  if (out_location == GVR_MEM_HOST) {
+    e = cudaMemcpyAsync(rgba, d_rgba, sizeof(float4) * pixels * n_views, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(depth, d_depth, sizeof(float) * pixels * n_views, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return cuda_error(e, "copy images to host");
+  }
+  if (samples_out) {
+    unsigned long long n = 0;
+    e = cudaMemcpyAsync(&n, s->d_counters, sizeof(n), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "read sample counter");
+    *samples_out = n;
+  } else if (out_location == GVR_MEM_HOST || !stream) {
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "batch render");
+  }
+  return GVR_OK;
+}
+
+int gvr_scene_batch_graph_builds(const gvr_scene *s, int *n)
+{
+  if (!s || !n) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = s->batch_graph_builds;
   return GVR_OK;
 }
 

@@ -56,6 +56,7 @@ struct Tuning {
   int packet_w = 8;
   int unroll = 2;
   int min_blocks = 4;
+  int tiles_per_item = 1;   // batch path: 16x16 tiles per work-queue item
 };
 
 // Everything the march kernel needs for one view.
@@ -147,6 +148,20 @@ struct gvr_scene {
   std::vector<float> classify_lut;
   float classify_smin = 0.f, classify_inv_range = 0.f;
   int classify_filter = -1;
+  // batched renders: per-view constants, per-(view, domain) screen rects,
+  // the work-queue counter, and the captured graph of the last batch shape
+  gvr::ViewDev *d_views = nullptr;
+  int views_cap = 0;
+  int4 *d_rects = nullptr;
+  int rects_cap = 0;
+  unsigned int *d_queue = nullptr;
+  float4 *d_batch_rgba = nullptr;
+  float *d_batch_depth = nullptr;
+  int64_t batch_pixels = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaGraphExec_t batch_exec = nullptr;
+  std::vector<unsigned char> batch_key;
+  int batch_graph_builds = 0;
 };
 
 namespace gvr {
@@ -196,5 +211,11 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          float4 *d_rgba, float *d_depth,
                          unsigned long long *d_samples, const Tuning &tuning,
                          bool has_hex, cudaStream_t stream);
+cudaError_t batch_grid(const MarchParams &mp, int n_views, const Tuning &tuning, bool has_hex,
+                       int *grid);
+cudaError_t launch_batch(const DomainDev *d_domains, const ViewDev *d_views, const int4 *d_rects,
+                         const MarchParams &mp, int n_views, const float4 *d_lut, float4 *d_rgba,
+                         float *d_depth, unsigned long long *d_samples, unsigned int *d_queue,
+                         const Tuning &tuning, bool has_hex, int grid, cudaStream_t stream);
 
 }  // namespace gvr

@@ -18,6 +18,7 @@
 // Domains are visited in increasing exit distance along each ray, which is
 // the order the reference's (pixel, depth) sort produces, so no partial
 // buffer or sort pass is needed.
+#include <algorithm>
 #include <cfloat>
 
 #include "gvr_hex_device.cuh"
@@ -325,6 +326,114 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
   return count;
 }
 
+// Everything one ray does: march the candidate domains (bits of `mask`) in
+// increasing exit distance, blend their partials, and finish the pixel
+// (image depth, uint8 round trip, background). Returns the samples taken.
+template <int UNROLL, bool HEX>
+__device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, const ViewDev &view,
+                                          const MarchParams &mp, const float4 *lut, int px, int py,
+                                          float4 &out, float &dep)
+{
+  int count = 0;
+  Ray r;
+  const float fx = view.dx_scale * ((float)px - 0.5f * (float)mp.width - view.xoff);
+  const float fy = view.dy_scale * ((float)py - 0.5f * (float)mp.height - view.yoff);
+  float d[3], dn = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    d[a] = view.look[a] + view.ru[a] * fx + view.rv[a] * fy;
+    dn = fmaf(d[a], d[a], dn);
+  }
+  const float inv = rsqrtf(dn);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    r.o[a] = view.origin[a];
+    r.d[a] = d[a] * inv;
+  }
+
+  float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f;
+  bool have = false;
+  float last_t1 = -FLT_MAX;
+  int last_d = -1;
+  for (;;) {
+    if (ca >= mp.early_term) break;
+    // next domain along the ray by (exit distance, index)
+    int best = -1;
+    float bt0 = 0.f, bt1 = FLT_MAX;
+    for (uint64_t m = mask; m; m &= m - 1) {
+      const int dd = __ffsll((long long)m) - 1;
+      float t0, t1;
+      if (!slab(doms[dd], r, t0, t1)) continue;
+      const bool after = t1 > last_t1 || (t1 == last_t1 && dd > last_d);
+      const bool before = best < 0 || t1 < bt1;
+      if (after && before) { best = dd; bt0 = t0; bt1 = t1; }
+    }
+    if (best < 0) break;
+    last_t1 = bt1;
+    last_d = best;
+    const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const DomainDev &dm = doms[best];
+    if (HEX && dm.kind == GVR_DOMAIN_HEX)
+      count += march_hex(dm, r, bt0, bt1, mp, lut, thr, acc);
+    else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
+             !(mp.skip_empty && *dm.any_empty))
+      count += march_uniform<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
+    else
+      count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
+    if (acc.w < mp.alpha_cull) continue;
+    if (!have) {
+      crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
+      cdepth = bt1;
+      have = true;
+    } else if (ca < 1.f && acc.w != 0.f) {
+      const float op = 1.f - ca;
+      crgb[0] = fmaf(op, acc.x, crgb[0]);
+      crgb[1] = fmaf(op, acc.y, crgb[1]);
+      crgb[2] = fmaf(op, acc.z, crgb[2]);
+      ca = fminf(fmaf(op, acc.w, ca), 1.f);
+    }
+  }
+
+  out = make_float4(0.f, 0.f, 0.f, 0.f);
+  dep = mp.clear_depth;
+  if (have) {
+    out = make_float4(crgb[0], crgb[1], crgb[2], ca);
+    // partials_to_canvas ray rebuild: delta_y runs along ru there
+    const float ex = view.dx_scale * (float)(2 * px - mp.width) * 0.5f;
+    const float ey = view.dy_scale * (float)(2 * py - mp.height) * 0.5f;
+    float q[3], qn = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      q[a] = view.look[a] + view.ru[a] * ex + view.ru[a] * ey;
+      qn = fmaf(q[a], q[a], qn);
+    }
+    const float qi = rsqrtf(qn);
+    float pos[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] = fmaf(cdepth, q[a] * qi, view.origin[a]);
+    const float *M = view.projview;
+    const float z = M[8] * pos[0] + M[9] * pos[1] + M[10] * pos[2] + M[11];
+    const float wv = M[12] * pos[0] + M[13] * pos[1] + M[14] * pos[2] + M[15];
+    dep = 0.5f * (z / wv) + 0.49f;
+  }
+  if (mp.quantize_uint8) {
+    out.x = (float)(unsigned char)fminf(out.x * 255.f, 255.f) * (1.f / 255.f);
+    out.y = (float)(unsigned char)fminf(out.y * 255.f, 255.f) * (1.f / 255.f);
+    out.z = (float)(unsigned char)fminf(out.z * 255.f, 255.f) * (1.f / 255.f);
+    out.w = (float)(unsigned char)fminf(out.w * 255.f, 255.f) * (1.f / 255.f);
+    dep = fabsf(dep);
+  }
+  if (mp.render_bg) {
+    const float om = 1.f - out.w;
+    out.x = fmaf(mp.bg[0], om, out.x);
+    out.y = fmaf(mp.bg[1], om, out.y);
+    out.z = fmaf(mp.bg[2], om, out.z);
+    out.w = fmaf(mp.bg[3], om, out.w);
+  }
+  return count;
+}
+
 // PW x (32 / PW) pixel packet per warp, 16 x 16 pixels per CTA.
 template <int PW, int UNROLL, int MINB, bool HEX = false>
 __global__ void __launch_bounds__(kThreads, MINB)
@@ -353,104 +462,95 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
   const bool valid = px < mp.width && py < mp.height;
   int count = 0;
   if (valid) {
-    Ray r;
-    const float fx = view.dx_scale * ((float)px - 0.5f * (float)mp.width - view.xoff);
-    const float fy = view.dy_scale * ((float)py - 0.5f * (float)mp.height - view.yoff);
-    float d[3], dn = 0.f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      d[a] = view.look[a] + view.ru[a] * fx + view.rv[a] * fy;
-      dn = fmaf(d[a], d[a], dn);
-    }
-    const float inv = rsqrtf(dn);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      r.o[a] = view.origin[a];
-      r.d[a] = d[a] * inv;
-    }
-
-    float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f;
-    bool have = false;
-    float last_t1 = -FLT_MAX;
-    int last_d = -1;
-    for (;;) {
-      if (ca >= mp.early_term) break;
-      // next domain along the ray by (exit distance, index)
-      int best = -1;
-      float bt0 = 0.f, bt1 = FLT_MAX;
-      for (int dd = 0; dd < mp.n_domains; ++dd) {
-        float t0, t1;
-        if (!slab(doms[dd], r, t0, t1)) continue;
-        const bool after = t1 > last_t1 || (t1 == last_t1 && dd > last_d);
-        const bool before = best < 0 || t1 < bt1;
-        if (after && before) { best = dd; bt0 = t0; bt1 = t1; }
-      }
-      if (best < 0) break;
-      last_t1 = bt1;
-      last_d = best;
-      const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      const DomainDev &dm = doms[best];
-      if (HEX && dm.kind == GVR_DOMAIN_HEX)
-        count += march_hex(dm, r, bt0, bt1, mp, lut, thr, acc);
-      else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
-               !(mp.skip_empty && *dm.any_empty))
-        count += march_uniform<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
-      else
-        count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
-      if (acc.w < mp.alpha_cull) continue;
-      if (!have) {
-        crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
-        cdepth = bt1;
-        have = true;
-      } else if (ca < 1.f && acc.w != 0.f) {
-        const float op = 1.f - ca;
-        crgb[0] = fmaf(op, acc.x, crgb[0]);
-        crgb[1] = fmaf(op, acc.y, crgb[1]);
-        crgb[2] = fmaf(op, acc.z, crgb[2]);
-        ca = fminf(fmaf(op, acc.w, ca), 1.f);
-      }
-    }
-
-    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    float dep = mp.clear_depth;
-    if (have) {
-      out = make_float4(crgb[0], crgb[1], crgb[2], ca);
-      // partials_to_canvas ray rebuild: delta_y runs along ru there
-      const float ex = view.dx_scale * (float)(2 * px - mp.width) * 0.5f;
-      const float ey = view.dy_scale * (float)(2 * py - mp.height) * 0.5f;
-      float q[3], qn = 0.f;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        q[a] = view.look[a] + view.ru[a] * ex + view.ru[a] * ey;
-        qn = fmaf(q[a], q[a], qn);
-      }
-      const float qi = rsqrtf(qn);
-      float pos[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) pos[a] = fmaf(cdepth, q[a] * qi, view.origin[a]);
-      const float *M = view.projview;
-      const float z = M[8] * pos[0] + M[9] * pos[1] + M[10] * pos[2] + M[11];
-      const float wv = M[12] * pos[0] + M[13] * pos[1] + M[14] * pos[2] + M[15];
-      dep = 0.5f * (z / wv) + 0.49f;
-    }
-    if (mp.quantize_uint8) {
-      out.x = (float)(unsigned char)fminf(out.x * 255.f, 255.f) * (1.f / 255.f);
-      out.y = (float)(unsigned char)fminf(out.y * 255.f, 255.f) * (1.f / 255.f);
-      out.z = (float)(unsigned char)fminf(out.z * 255.f, 255.f) * (1.f / 255.f);
-      out.w = (float)(unsigned char)fminf(out.w * 255.f, 255.f) * (1.f / 255.f);
-      dep = fabsf(dep);
-    }
-    if (mp.render_bg) {
-      const float om = 1.f - out.w;
-      out.x = fmaf(mp.bg[0], om, out.x);
-      out.y = fmaf(mp.bg[1], om, out.y);
-      out.z = fmaf(mp.bg[2], om, out.z);
-      out.w = fmaf(mp.bg[3], om, out.w);
-    }
+    const uint64_t all = mp.n_domains >= 64 ? ~0ull : ((1ull << mp.n_domains) - 1ull);
+    float4 out;
+    float dep;
+    count = render_ray<UNROLL, HEX>(doms, all, view, mp, lut, px, py, out, dep);
     const int64_t pix = (int64_t)py * mp.width + px;
     rgba[pix] = out;
     depth[pix] = dep;
+  }
+  if (samples) {
+    unsigned long long c = (unsigned long long)count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0 && c) atomicAdd(samples, c);
+  }
+}
+
+
+// Many views in one persistent launch. A device counter hands out work items
+// of `tiles_per_item` consecutive 16x16 tiles; items run through every tile
+// of view 0, then view 1, ... so neighbouring CTAs share bricks in L2. Each
+// tile first builds the bitmask of domains whose projected screen rectangle
+// (rects[view * n_domains + d], inclusive pixel bounds, computed on the host)
+// touches it, and its rays march only those. The counter only grows: no CTA
+// ever waits for another.
+template <int PW, int UNROLL, int MINB, bool HEX>
+__global__ void __launch_bounds__(kThreads, MINB)
+batch_kernel(const DomainDev *__restrict__ g_domains, const ViewDev *__restrict__ views,
+             const int4 *__restrict__ rects, const MarchParams mp, int n_views, int tiles_x,
+             int tiles_y, int tiles_per_item, const float4 *__restrict__ g_lut,
+             float4 *__restrict__ rgba, float *__restrict__ depth,
+             unsigned long long *__restrict__ samples, unsigned int *__restrict__ queue)
+{
+  constexpr int PH = 32 / PW;
+  constexpr int PX = kTile / PW;
+  extern __shared__ float4 smem[];
+  float4 *lut = smem;
+  DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
+  __shared__ unsigned int s_item;
+  __shared__ unsigned int s_mask[2];
+  for (int i = threadIdx.x; i < mp.lut_size; i += kThreads) lut[i] = g_lut[i];
+  {
+    const int words = mp.n_domains * (int)(sizeof(DomainDev) / 4);
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(g_domains);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(doms);
+    for (int i = threadIdx.x; i < words; i += kThreads) dst[i] = src[i];
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tiles_per_view = tiles_x * tiles_y;
+  const long long total_tiles = (long long)tiles_per_view * n_views;
+  const long long n_items = (total_tiles + tiles_per_item - 1) / tiles_per_item;
+  const int64_t pixels = (int64_t)mp.width * mp.height;
+  int count = 0;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1u);
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= n_items) break;
+    for (int sub = 0; sub < tiles_per_item; ++sub) {
+      const long long tile = item * tiles_per_item + sub;
+      if (tile >= total_tiles) break;
+      const int v = (int)(tile / tiles_per_view);
+      const int t = (int)(tile % tiles_per_view);
+      const int tx = t % tiles_x, ty = t / tiles_x;
+      const int x0 = tx * kTile, y0 = ty * kTile;
+      if (warp < 2) {
+        const int d = warp * 32 + lane;
+        bool hit = false;
+        if (d < mp.n_domains) {
+          const int4 r = __ldg(rects + (int64_t)v * mp.n_domains + d);
+          hit = !(r.z < x0 || r.x > x0 + kTile - 1 || r.w < y0 || r.y > y0 + kTile - 1);
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) s_mask[warp] = b;
+      }
+      __syncthreads();
+      const uint64_t mask = ((uint64_t)s_mask[1] << 32) | s_mask[0];
+      const int px = x0 + (warp % PX) * PW + (lane % PW);
+      const int py = y0 + (warp / PX) * PH + (lane / PW);
+      if (px < mp.width && py < mp.height) {
+        float4 out;
+        float dep;
+        count += render_ray<UNROLL, HEX>(doms, mask, views[v], mp, lut, px, py, out, dep);
+        const int64_t pix = (int64_t)v * pixels + (int64_t)py * mp.width + px;
+        rgba[pix] = out;
+        depth[pix] = dep;
+      }
+      __syncthreads();
+    }
   }
   if (samples) {
     unsigned long long c = (unsigned long long)count;
@@ -501,6 +601,75 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
   dim3 grid((mp.width + kTile - 1) / kTile, (mp.height + kTile - 1) / kTile);
   fn<<<grid, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba, d_depth, d_samples);
   count_launch();
+  return cudaGetLastError();
+}
+
+
+namespace {
+
+using BatchFn = void (*)(const DomainDev *, const ViewDev *, const int4 *, const MarchParams, int,
+                         int, int, int, const float4 *, float4 *, float *, unsigned long long *,
+                         unsigned int *);
+
+BatchFn select_batch(const Tuning &t, bool has_hex)
+{
+  if (has_hex) return t.packet_w == 4 ? batch_kernel<4, 1, 2, true> : batch_kernel<8, 1, 2, true>;
+  const int u = t.unroll >= 2 ? 2 : 1;
+  const int m = t.min_blocks >= 4 ? 4 : 3;
+  switch (t.packet_w) {
+    case 4:
+      return u == 2 ? (m == 4 ? batch_kernel<4, 2, 4, false> : batch_kernel<4, 2, 3, false>)
+                    : (m == 4 ? batch_kernel<4, 1, 4, false> : batch_kernel<4, 1, 3, false>);
+    case 16:
+      return u == 2 ? (m == 4 ? batch_kernel<16, 2, 4, false> : batch_kernel<16, 2, 3, false>)
+                    : (m == 4 ? batch_kernel<16, 1, 4, false> : batch_kernel<16, 1, 3, false>);
+    default:
+      return u == 2 ? (m == 4 ? batch_kernel<8, 2, 4, false> : batch_kernel<8, 2, 3, false>)
+                    : (m == 4 ? batch_kernel<8, 1, 4, false> : batch_kernel<8, 1, 3, false>);
+  }
+}
+
+}  // namespace
+
+// Resident CTAs of the batch kernel for this launch shape (SMs x CTAs per SM
+// from the occupancy calculator), capped by the number of work items. Also
+// sets the kernel's dynamic shared-memory limit; call it outside any capture.
+cudaError_t batch_grid(const MarchParams &mp, int n_views, const Tuning &tuning, bool has_hex,
+                       int *grid)
+{
+  const size_t smem = sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains;
+  BatchFn fn = select_batch(tuning, has_hex);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(float4) * kMaxLut + sizeof(DomainDev) * kMaxDomains));
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem);
+  if (e != cudaSuccess) return e;
+  const int tiles_x = (mp.width + kTile - 1) / kTile, tiles_y = (mp.height + kTile - 1) / kTile;
+  const int tpi = tuning.tiles_per_item > 0 ? tuning.tiles_per_item : 1;
+  const long long items = ((long long)tiles_x * tiles_y * n_views + tpi - 1) / tpi;
+  *grid = (int)std::max(1ll, std::min<long long>(items, (long long)sms * std::max(per_sm, 1)));
+  return cudaSuccess;
+}
+
+// Clear the work counter and launch the persistent batch kernel (both stream
+// operations, so the pair can be captured into a CUDA graph).
+cudaError_t launch_batch(const DomainDev *d_domains, const ViewDev *d_views, const int4 *d_rects,
+                         const MarchParams &mp, int n_views, const float4 *d_lut, float4 *d_rgba,
+                         float *d_depth, unsigned long long *d_samples, unsigned int *d_queue,
+                         const Tuning &tuning, bool has_hex, int grid, cudaStream_t stream)
+{
+  const size_t smem = sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains;
+  BatchFn fn = select_batch(tuning, has_hex);
+  const int tiles_x = (mp.width + kTile - 1) / kTile, tiles_y = (mp.height + kTile - 1) / kTile;
+  const int tpi = tuning.tiles_per_item > 0 ? tuning.tiles_per_item : 1;
+  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned int), stream);
+  if (e != cudaSuccess) return e;
+  fn<<<(unsigned)grid, kThreads, smem, stream>>>(d_domains, d_views, d_rects, mp, n_views, tiles_x,
+                                                 tiles_y, tpi, d_lut, d_rgba, d_depth, d_samples,
+                                                 d_queue);
   return cudaGetLastError();
 }
 

@@ -169,6 +169,44 @@ class Scene:
             return rgba, depth, int(n.value)
         return rgba, depth
 
+    def render_batch(self, cameras, params: N.RenderParams, *, device_out=False, stream=None,
+                     count_samples=False, out=None):
+        """Render many views in one persistent, graph-replayed launch. Returns
+        (rgba (V, H, W, 4), depth (V, H, W)) as numpy, or torch CUDA tensors when
+        device_out (then `out` may pass preallocated (rgba, depth) tensors)."""
+        cams = (N.Camera * len(cameras))(*cameras)
+        w, h, v = params.width, params.height, len(cameras)
+        n = C.c_uint64(0)
+        nptr = C.byref(n) if count_samples else None
+        st = C.c_void_p(stream) if stream is not None else None
+        if device_out:
+            import torch
+            if out is None:
+                out = (torch.empty((v, h, w, 4), dtype=torch.float32, device=f"cuda:{self.device}"),
+                       torch.empty((v, h, w), dtype=torch.float32, device=f"cuda:{self.device}"))
+            rgba, depth = out
+            if stream is None:
+                st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            N.call("gvr_render_volume_batch", self.handle, cams, v, C.byref(params),
+                   C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, st, nptr)
+        else:
+            rgba = np.empty((v, h, w, 4), dtype=np.float32)
+            depth = np.empty((v, h, w), dtype=np.float32)
+            N.call("gvr_render_volume_batch", self.handle, cams, v, C.byref(params),
+                   C.c_void_p(rgba.ctypes.data), C.c_void_p(depth.ctypes.data), N.MEM_HOST, st, nptr)
+        if count_samples:
+            return rgba, depth, int(n.value)
+        return rgba, depth
+
+    def set_batch_granularity(self, tiles_per_item: int) -> None:
+        N.call("gvr_scene_set_batch_granularity", self.handle, int(tiles_per_item))
+
+    @property
+    def batch_graph_builds(self) -> int:
+        n = C.c_int()
+        N.call("gvr_scene_batch_graph_builds", self.handle, C.byref(n))
+        return n.value
+
     def close(self) -> None:
         if self.handle:
             N.lib().gvr_scene_destroy(self.handle)

@@ -192,6 +192,72 @@ def hex_mesh(n_cells: int = 200, seed: int = 3, width: int = 1024, height: int =
                     rp, rgb, ap, al)
 
 
+EDGES = (32, 48, 64, 96, 128, 192, 256)
+
+
+def kd_boxes(root, n_boxes: int, rng: np.random.Generator) -> list:
+    """Split the integer box `root` = (x0, y0, z0, x1, y1, z1) (cells) into
+    n_boxes boxes: repeatedly split the largest box along a random axis at an
+    offset that leaves both parts with edge lengths in EDGES."""
+    boxes = [tuple(root)]
+    while len(boxes) < n_boxes:
+        order = sorted(range(len(boxes)), key=lambda i: -np.prod(
+            [boxes[i][3 + a] - boxes[i][a] for a in range(3)]))
+        for i in order:
+            b = boxes[i]
+            axes = rng.permutation(3)
+            done = False
+            for a in axes:
+                L = b[3 + a] - b[a]
+                cuts = [e for e in EDGES if (L - e) in EDGES]
+                if cuts:
+                    e = int(rng.choice(cuts))
+                    lo = list(b)
+                    hi = list(b)
+                    lo[3 + a] = b[a] + e
+                    hi[a] = b[a] + e
+                    boxes[i:i + 1] = [tuple(lo), tuple(hi)]
+                    done = True
+                    break
+            if done:
+                break
+        else:
+            raise ValueError("cannot split further with the allowed edge lengths")
+    return boxes
+
+
+def cinema_batch(n_domains: int = 37, box_cells: int = 256, seed: int = 4, width: int = 512,
+                 height: int = 512, n_phi: int = 8, n_theta: int = 8) -> Workload:
+    """n_domains uniform float32 domains of uneven sizes (edges from
+    {32,48,64,96,128,192,256} cells per axis, seeded k-d splits) tiling a
+    box_cells^3 box of one Gaussian-blob field (nodes shared across faces),
+    spacing 1/box_cells; rendered for n_phi x n_theta Cinema cameras."""
+    rng = np.random.default_rng(seed)
+    boxes = kd_boxes((0, 0, 0, box_cells, box_cells, box_cells), n_domains, rng)
+    c, s, a = blob_params(rng)
+    h = 1.0 / box_cells
+    doms = []
+    for b in boxes:
+        coords = [np.arange(b[ax], b[3 + ax] + 1) * h for ax in range(3)]
+        f = blob_field(coords, c, s, a)
+        doms.append(UniformDomain(f, (b[0] * h, b[1] * h, b[2] * h), (h, h, h)))
+    samples = int(np.ceil(np.sqrt(3.0) * box_cells / 0.5))
+    rp, rgb, ap, al = linear_ramp_tf()
+    wl = Workload(f"cinema{n_domains}dom{box_cells}^3x{n_phi * n_theta}views@{width}x{height}", doms,
+                  width, height, samples, 0.0, 0.0, rp, rgb, ap, al)
+    wl.phi_theta = cinema_angles(n_phi, n_theta)
+    return wl
+
+
+def cinema_angles(n_phi: int, n_theta: int) -> np.ndarray:
+    """(phi, theta) pairs of a Cinema sweep given `phi`/`theta` counts:
+    phi from -180 in steps of 360/n_phi, theta from 0 in steps of 180/n_theta
+    (CinemaManager, ascent_runtime_rendering_filters.cpp:555-610)."""
+    phis = [-180.0 + i * 360.0 / n_phi for i in range(n_phi)]
+    thetas = [0.0 + j * 180.0 / n_theta for j in range(n_theta)]
+    return np.array([(p, t) for p in phis for t in thetas], dtype=np.float32)
+
+
 def plain_large(n_cells: int = 512, seed: int = 2, width: int = 1024, height: int = 1024,
                 parts=(2, 2, 2)) -> Workload:
     """A (n_cells+1)^3-node float32 field (Gaussian blobs + 3-octave sinusoidal turbulence)

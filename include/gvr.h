@@ -271,6 +271,29 @@ GVR_API int gvr_render_volume(gvr_scene *scene, const gvr_camera *camera,
                       float *depth, int out_location, void *stream,
                       uint64_t *samples_out);
 
+/* Render n_views cameras of the scene in one persistent launch: rgba holds
+ * n_views images of 4*W*H floats and depth n_views images of W*H floats,
+ * view-major, each image exactly what gvr_render_volume returns for that
+ * camera. A device work queue hands out (view, tile) items; each 16x16 tile
+ * marches only the domains whose projected bounds touch it. The counter
+ * reset and the launch are captured as a CUDA graph, rebuilt only when the
+ * launch configuration (parameters, view count, buffers, launch shape)
+ * changes. Replaces the per-view loop of vtkh::Scene::Render over Cinema
+ * cameras (Scene.cpp:124-247, ascent_runtime_rendering_filters.cpp:906-960).
+ * With stream NULL the call uses a scene-owned stream and waits for it. */
+GVR_API int gvr_render_volume_batch(gvr_scene *scene, const gvr_camera *cameras, int n_views,
+                                    const gvr_render_params *params, float *rgba,
+                                    float *depth, int out_location, void *stream,
+                                    uint64_t *samples_out);
+
+/* Work-queue granularity of the batch path: 16x16 tiles per item (1..64);
+ * set by the autotuner. No counterpart in the reference. */
+GVR_API int gvr_scene_set_batch_granularity(gvr_scene *scene, int tiles_per_item);
+
+/* Number of CUDA graphs the batch path has captured for this scene (a
+ * diagnostic; no counterpart in the reference). */
+GVR_API int gvr_scene_batch_graph_builds(const gvr_scene *scene, int *n);
+
 /* Render one uniform domain without allocating any device memory; no
  * counterpart in the reference. For callers that may not call cudaMalloc or
  * cudaFree — typically a simulation that gives all GPU memory to its own
