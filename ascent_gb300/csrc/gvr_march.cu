@@ -15,9 +15,9 @@
 //     0.5 z/w + 0.49                        (VolumeRenderer.cpp:287-391),
 //   - the uint8 round trip of the single-domain path (Image.hpp:102-105,
 //     Renderer.cpp:265-283) and the background blend.
-// Domains are visited in increasing exit distance along each ray, which is
-// the order the reference's (pixel, depth) sort produces, so no partial
-// buffer or sort pass is needed.
+// Domains are visited in increasing entry distance along each ray, which for
+// disjoint boxes is the order the reference's (pixel, exit depth) sort
+// produces, so no partial buffer or sort pass is needed.
 #include <algorithm>
 #include <cfloat>
 
@@ -353,24 +353,31 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
 
   float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f;
   bool have = false;
-  float last_t1 = -FLT_MAX;
+  float last_t0 = -FLT_MAX, covered = -FLT_MAX;
   int last_d = -1;
   for (;;) {
     if (ca >= mp.early_term) break;
-    // next domain along the ray by (exit distance, index)
+    // Next domain along the ray by (entry distance, index). Domains tile
+    // space without overlapping, so each is marched from the furthest exit
+    // reached so far: every point of the ray is covered once, also where
+    // rounding makes neighbouring intervals overlap (rays lying in a shared
+    // face). For disjoint boxes this is the order of the reference's
+    // (pixel, depth = exit distance) sort.
     int best = -1;
-    float bt0 = 0.f, bt1 = FLT_MAX;
+    float bt0 = FLT_MAX, bt1 = 0.f;
     for (uint64_t m = mask; m; m &= m - 1) {
       const int dd = __ffsll((long long)m) - 1;
       float t0, t1;
       if (!slab(doms[dd], r, t0, t1)) continue;
-      const bool after = t1 > last_t1 || (t1 == last_t1 && dd > last_d);
-      const bool before = best < 0 || t1 < bt1;
+      const bool after = t0 > last_t0 || (t0 == last_t0 && dd > last_d);
+      const bool before = best < 0 || t0 < bt0;
       if (after && before) { best = dd; bt0 = t0; bt1 = t1; }
     }
     if (best < 0) break;
-    last_t1 = bt1;
+    last_t0 = bt0;
     last_d = best;
+    bt0 = fmaxf(bt0, covered);
+    covered = fmaxf(covered, bt1);
     const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const DomainDev &dm = doms[best];

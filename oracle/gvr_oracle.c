@@ -41,7 +41,13 @@
  *   A4 LUT lookup nearest: idx = (int)(s (N-1)); linear: lerp at s (N-1);
  *   A5 front-to-back blend C += (1-A) a c, A += (1-A) a;
  *   A6 optional early termination once the composited alpha reaches
- *      early_term (>= 1 disables it).
+ *      early_term (>= 1 disables it);
+ *   A7 domains do not overlap (Ascent strips ghost zones before plots):
+ *      along a ray they are visited in order of entry distance and each is
+ *      marched from the furthest exit reached so far, so every point is
+ *      covered once even where rounding makes neighbouring intervals overlap
+ *      (rays in a shared face); for disjoint boxes this is the order of the
+ *      reference's (pixel, exit depth) sort.
  */
 #include <math.h>
 #include <stdint.h>
@@ -1007,10 +1013,11 @@ static REAL image_depth(const or_basis *b, const double M[4][4], int W, int H,
   return (REAL)(0.5 * (np[2] / np[3]) + 0.49);
 }
 
+/* Domain order along a ray: entry distance (stashed in .alpha), then index. */
 static int cmp_rpartial(const void *pa, const void *pb)
 {
   const or_rpartial *a = (const or_rpartial *)pa, *b = (const or_rpartial *)pb;
-  if (a->depth != b->depth) return a->depth < b->depth ? -1 : 1;
+  if (a->alpha != b->alpha) return a->alpha < b->alpha ? -1 : 1;
   return a->dom - b->dom;
 }
 
@@ -1051,9 +1058,14 @@ int or_render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_pa
       qsort(parts, np, sizeof(or_rpartial), cmp_rpartial);
       REAL rgb[3] = {0, 0, 0}, a = 0, front_depth = 0;
       int have = 0;
+      REAL covered = -INFINITY;
       for (int k = 0; k < np; ++k) {
         REAL acc[4] = {0, 0, 0, 0};
         REAL t0 = parts[k].alpha, t1 = parts[k].depth;
+        /* A7: domains in entry order, each marched from the furthest exit
+         * reached so far */
+        if (t0 < covered) t0 = covered;
+        if (t1 > covered) covered = t1;
         if (p->early_term < 1 && a >= (REAL)p->early_term) break;
         total += (uint64_t)march(&s->d[parts[k].dom], b.origin, dir, t0, t1, p, a, acc);
         if (acc[3] < (REAL)p->alpha_cull) continue;
