@@ -108,6 +108,13 @@ class Scene:
         out["build_ms"] = ms.value
         return out
 
+    def hex_build_ms(self, domain_id: int) -> float:
+        """Wall time of the domain's on-device LBVH build (upload included)."""
+        ms = C.c_float(0)
+        N.call("gvr_scene_hex_bvh", self.handle, int(domain_id), None, None, None, None, None, None,
+               C.byref(ms))
+        return ms.value
+
     def hex_cells(self, domain_id: int) -> int:
         return int(self._hex_cells[domain_id])
 

@@ -48,6 +48,41 @@ def _time(scene, camera, params, rgba, depth, stream, reps: int) -> float:
     return statistics.median(times)
 
 
+GRANULARITY = (1, 2, 4, 8)
+
+
+def autotune_batch(scene, cameras, params, reps: int = 2) -> dict:
+    """Pick launch shape and work-queue granularity (16x16 tiles per item) for
+    the persistent batch path on these views; returns {"best", "ms"}."""
+    import torch
+    v = len(cameras)
+    dev = f"cuda:{scene.device}"
+    out = (torch.empty((v, params.height, params.width, 4), dtype=torch.float32, device=dev),
+           torch.empty((v, params.height, params.width), dtype=torch.float32, device=dev))
+    stream = torch.cuda.current_stream(scene.device)
+    results = {}
+    for cand in CANDIDATES:
+        for g in GRANULARITY:
+            scene.set_tuning(**cand)
+            scene.set_batch_granularity(g)
+            scene.render_batch(cameras, params, device_out=True, out=out)  # capture + warm
+            times = []
+            for _ in range(reps):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                scene.render_batch(cameras, params, device_out=True, out=out)
+                b.record(stream)
+                b.synchronize()
+                times.append(a.elapsed_time(b))
+            results[f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}g{g}"] = (
+                statistics.median(times), cand, g)
+    name, (ms, best, g) = min(results.items(), key=lambda kv: kv[1][0])
+    scene.set_tuning(**best)
+    scene.set_batch_granularity(g)
+    return {"best": dict(best, tiles_per_item=g), "ms": {k: round(r[0], 4) for k, r in results.items()}}
+
+
 def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True) -> dict:
     """Pick and set the fastest launch shape for this scene and view; returns
     {"best": shape, "ms": {shape-string: median ms}, "cached": bool}."""

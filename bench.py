@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the hexahedral and batched-view configurations")
     return ap.parse_args()
 
 
@@ -180,6 +182,108 @@ def cpu_sample(wl, cam, params, seconds: float, per_step: bool = False):
     return {"value": samples / dt / 1e9, "unit": UNIT, "cores": O.num_threads(32), "kind": "port",
             "sample": f"{rows} of {h} image rows (central bands) of the same view, "
                       f"{samples} samples in {dt:.1f} s, FP32 OpenMP port of the oracle"}, osc
+
+
+def _timed(fn, stream, reps):
+    """Median ms of `reps` calls of fn, CUDA events on `stream`."""
+    import torch
+    times = []
+    for _ in range(reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return statistics.median(times)
+
+
+def bench_hex(dev, n_cells=200, size=1024, reps=5):
+    """Unstructured hexahedra: jittered n_cells^3 grid, device LBVH + Newton march."""
+    import ctypes as C
+    import torch
+    from ascent_gb300 import _native as N
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import volume as V
+    from ascent_gb300 import workloads as W
+    t0 = time.time()
+    wl = W.hex_mesh(n_cells=n_cells, width=size, height=size)
+    gen_s = time.time() - t0
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    sc = S.Scene(dev)
+    t0 = time.time()
+    V.load_workload(sc, wl)
+    load_s = time.time() - t0
+    build_ms = sc.hex_build_ms(0)
+    stream = torch.cuda.current_stream(dev)
+    rgba = torch.empty((size, size, 4), dtype=torch.float32, device=f"cuda:{dev}")
+    depth = torch.empty((size, size), dtype=torch.float32, device=f"cuda:{dev}")
+    _, _, n = sc.render(cam, p, device_out=True, count_samples=True)
+    args = (sc.handle, C.byref(cam), C.byref(p), C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()),
+            N.MEM_DEVICE, C.c_void_p(stream.cuda_stream), None)
+    for _ in range(2):
+        N.call("gvr_render_volume", *args)
+    ms = _timed(lambda: N.call("gvr_render_volume", *args), stream, reps)
+    pk = peaks()
+    alg = n * 160 + size * size * BYTES_PER_PIXEL
+    sc.close()
+    return {"workload": wl.name, "cells": n_cells ** 3, "samples_per_frame": n,
+            "gsamples_per_s": n / ms / 1e6, "fps": 1e3 / ms, "ms_per_frame": ms,
+            "bvh_build_ms": build_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
+            "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": pk["hbm_gbs"],
+                         "unit": "GB/s", "frac": alg / ms / 1e6 / pk["hbm_gbs"],
+                         "bytes_per_sample": 160}}
+
+
+def bench_batch(dev, reps=5):
+    """37 uneven uniform domains, 64 Cinema views at 512^2: one persistent
+    graph-replayed batch launch vs the plain per-view loop (device images)."""
+    import ctypes as C
+    import torch
+    from ascent_gb300 import _native as N
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import tune
+    from ascent_gb300 import volume as V
+    from ascent_gb300 import workloads as W
+    wl = W.cinema_batch()
+    cams = S.cinema_cameras(wl.bounds, wl.phi_theta)
+    p = V.workload_params(wl)
+    sc = S.Scene(dev)
+    V.load_workload(sc, wl)
+    stream = torch.cuda.current_stream(dev)
+    v, h, w = len(cams), p.height, p.width
+    out = (torch.empty((v, h, w, 4), dtype=torch.float32, device=f"cuda:{dev}"),
+           torch.empty((v, h, w), dtype=torch.float32, device=f"cuda:{dev}"))
+    # plain per-view loop, tuned for a single view
+    single = tune.autotune(sc, cams[0], p, reps=2, use_cache=False)["best"]
+    sptr = C.c_void_p(stream.cuda_stream)
+    stride4, stride1 = h * w * 4 * 4, h * w * 4
+    base4, base1 = out[0].data_ptr(), out[1].data_ptr()
+    calls = [(sc.handle, C.byref(cams[i]), C.byref(p), C.c_void_p(base4 + i * stride4),
+              C.c_void_p(base1 + i * stride1), N.MEM_DEVICE, sptr, None) for i in range(v)]
+
+    def loop():
+        for a in calls:
+            N.call("gvr_render_volume", *a)
+
+    loop()
+    loop_ms = _timed(loop, stream, reps)
+    ref = out[0].clone()
+    # batched: tuned launch shape and queue granularity
+    best = tune.autotune_batch(sc, cams, p, reps=2)
+    _, _, n = sc.render_batch(cams, p, device_out=True, out=out, count_samples=True)
+    batch_ms = _timed(lambda: sc.render_batch(cams, p, device_out=True, out=out), stream, reps)
+    same = bool(torch.equal(ref, out[0]))
+    builds = sc.batch_graph_builds
+    sc.close()
+    return {"workload": wl.name, "domains": len(wl.domains), "views": v, "image": [w, h],
+            "samples_per_batch": n, "per_view_loop_ms": loop_ms, "batched_ms": batch_ms,
+            "per_view_loop_images_per_s": v * 1e3 / loop_ms, "batched_images_per_s": v * 1e3 / batch_ms,
+            "speedup": loop_ms / batch_ms, "batched_gsamples_per_s": n / batch_ms / 1e6,
+            "images_identical_to_loop": same, "loop_tuning": single, "batch_tuning": best["best"],
+            "graph_captures": builds}
 
 
 def run_reference(args):
@@ -333,6 +437,12 @@ def run_ours(args):
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         cpu, _ = cpu_sample(wl, cam, params, args.cpu_seconds)
+    scene.close()
+    others = {}
+    if world == 1 and not args.no_configs:
+        torch.cuda.synchronize()
+        others["hex"] = bench_hex(dev)
+        others["batched"] = bench_batch(dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -361,9 +471,9 @@ def run_ours(args):
                 "steps": e2e_steps, "ms_per_step": e2e_s / e2e_steps * 1e3},
         "clocks": clk,
         "gpu_launches": launches,
+        "configs": others,
     }
     print(json.dumps(line), flush=True)
-    scene.close()
     if dist:
         dist.destroy_process_group()
     return 0
