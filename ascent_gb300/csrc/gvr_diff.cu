@@ -1,0 +1,449 @@
+// gvr_diff.cu — differentiable volume render: forward with transmittance
+// checkpoints and its hand-written adjoint.
+//
+// The render is the single-uniform-domain march of gvr_march.cu (same ray
+// model, stepping rule and front-to-back blend) with the two changes a
+// gradient needs: the transfer function is looked up with linear
+// interpolation (so colour and opacity are differentiable in the scalar),
+// and no partial is culled. Inputs are the caller's device buffers: the node
+// field in its plain layout (x fastest) and the LUT (n RGBA floats), both
+// differentiable.
+//
+// Forward: one thread per ray; every kDiffK samples it stores the
+// accumulated (rgb, alpha) at the start of the segment.
+// Backward: per ray, segments from last to first. A segment is re-marched
+// from its checkpoint, keeping each sample's transmittance T_k and scalar v_k
+// in thread-local arrays (the blend is never inverted); then its samples are
+// walked back to front with the suffix composite (R', A') of the samples
+// behind them:
+//   dL/dc_k = T_k a_k g_rgb,
+//   dL/da_k = T_k (g_rgb . (c_k - R'_k) + g_A (1 - A'_k)),
+//   R'_{k-1} = a_k c_k + (1 - a_k) R'_k,  A'_{k-1} = a_k + (1 - a_k) A'_k.
+// LUT gradients accumulate in shared memory per CTA; field gradients are
+// summed per ray while consecutive samples stay in one cell, then combined
+// across the lanes of a warp that hit the same cell (__match_any_sync) and
+// added to the eight corners with one atomic per distinct node.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "gvr_internal.h"
+
+namespace gvr {
+namespace {
+
+constexpr int kDiffK = 64;          // samples per transmittance checkpoint
+constexpr int kMaxDiffViews = 64;
+constexpr int kDiffLut = 4096;
+
+struct DiffViews {
+  ViewDev v[kMaxDiffViews];
+};
+
+struct DiffGrid {
+  int dims[3];
+  float origin[3];
+  float inv_spacing[3];
+  float lo[3];
+  float hi[3];
+};
+
+struct DiffParams {
+  int width;
+  int height;
+  int n_views;
+  int lut_size;
+  int n_seg;
+  float sample_dist;
+  float scalar_min;
+  float inv_range;
+};
+
+__device__ __forceinline__ float lerp2(float a, float b, float w) { return fmaf(w, b - a, a); }
+
+// Ray of pixel (px, py) of view v: origin, unit direction, [t0, t1) inside the
+// grid; false when the ray misses it.
+__device__ __forceinline__ bool diff_ray(const ViewDev &view, const DiffGrid &g, const DiffParams &p,
+                                         int px, int py, float o[3], float d[3], float &t0,
+                                         float &t1)
+{
+  const float fx = view.dx_scale * ((float)px - 0.5f * (float)p.width - view.xoff);
+  const float fy = view.dy_scale * ((float)py - 0.5f * (float)p.height - view.yoff);
+  float dn = 0.f;
+  for (int a = 0; a < 3; ++a) {
+    d[a] = view.look[a] + view.ru[a] * fx + view.rv[a] * fy;
+    dn = fmaf(d[a], d[a], dn);
+  }
+  const float inv = rsqrtf(dn);
+  t0 = 0.f;
+  t1 = FLT_MAX;
+  for (int a = 0; a < 3; ++a) {
+    o[a] = view.origin[a];
+    d[a] *= inv;
+    if (d[a] != 0.f) {
+      const float r = 1.f / d[a];
+      float ta = (g.lo[a] - o[a]) * r, tb = (g.hi[a] - o[a]) * r;
+      if (ta > tb) { const float t = ta; ta = tb; tb = t; }
+      t0 = fmaxf(t0, ta);
+      t1 = fminf(t1, tb);
+    } else if (o[a] < g.lo[a] || o[a] > g.hi[a]) {
+      return false;
+    }
+  }
+  return t1 > t0;
+}
+
+// Cell (linear index of its corner 000) and trilinear weights of sample t.
+__device__ __forceinline__ int64_t diff_cell(const DiffGrid &g, const float A[3], const float B[3],
+                                             float t, float w[3])
+{
+  int c[3];
+  for (int a = 0; a < 3; ++a) {
+    const float gg = fmaf(t, B[a], A[a]);
+    c[a] = max(0, min((int)gg, g.dims[a] - 2));
+    w[a] = gg - (float)c[a];
+  }
+  return ((int64_t)c[2] * g.dims[1] + c[1]) * g.dims[0] + c[0];
+}
+
+__device__ __forceinline__ float diff_value(const float *__restrict__ f, const DiffGrid &g,
+                                            int64_t base, const float w[3])
+{
+  const int64_t sy = g.dims[0], sz = (int64_t)g.dims[0] * g.dims[1];
+  const float *p = f + base;
+  const float c00 = lerp2(__ldg(p), __ldg(p + 1), w[0]);
+  const float c10 = lerp2(__ldg(p + sy), __ldg(p + sy + 1), w[0]);
+  const float c01 = lerp2(__ldg(p + sz), __ldg(p + sz + 1), w[0]);
+  const float c11 = lerp2(__ldg(p + sz + sy), __ldg(p + sz + sy + 1), w[0]);
+  return lerp2(lerp2(c00, c10, w[1]), lerp2(c01, c11, w[1]), w[2]);
+}
+
+// Linear LUT lookup at scalar v; also returns the entry index i0 and weight.
+__device__ __forceinline__ float4 diff_lut(const float4 *lut, const DiffParams &p, float v,
+                                           float &s_raw, int &i0, float &wl)
+{
+  s_raw = (v - p.scalar_min) * p.inv_range;
+  const float s = __saturatef(s_raw);
+  const float x = s * (float)(p.lut_size - 1);
+  i0 = min((int)x, p.lut_size - 2);
+  wl = x - (float)i0;
+  const float4 a = lut[i0], b = lut[i0 + 1];
+  return make_float4(lerp2(a.x, b.x, wl), lerp2(a.y, b.y, wl), lerp2(a.z, b.z, wl),
+                     lerp2(a.w, b.w, wl));
+}
+
+__global__ void __launch_bounds__(256)
+diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews views,
+             const DiffParams p, const float4 *__restrict__ g_lut, float4 *__restrict__ rgba,
+             float4 *__restrict__ ckpt)
+{
+  extern __shared__ float4 lut[];
+  for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) lut[i] = g_lut[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  const int py = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+  const int v = blockIdx.z;
+  if (px >= p.width || py >= p.height) return;
+  const int64_t ray = ((int64_t)v * p.height + py) * p.width + px;
+  float o[3], d[3], t0, t1;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (diff_ray(views.v[v], g, p, px, py, o, d, t0, t1)) {
+    float A[3], B[3];
+    for (int a = 0; a < 3; ++a) {
+      A[a] = (o[a] - g.origin[a]) * g.inv_spacing[a];
+      B[a] = d[a] * g.inv_spacing[a];
+    }
+    for (int k = 0;; ++k) {
+      const float t = fmaf((float)k, p.sample_dist, t0);
+      if (!(t < t1)) break;
+      if (ckpt && (k % kDiffK) == 0 && k / kDiffK < p.n_seg) ckpt[ray * p.n_seg + k / kDiffK] = acc;
+      float w[3];
+      const int64_t base = diff_cell(g, A, B, t, w);
+      const float val = diff_value(field, g, base, w);
+      float s_raw, wl;
+      int i0;
+      const float4 c = diff_lut(lut, p, val, s_raw, i0, wl);
+      const float wa = (1.f - acc.w) * c.w;
+      acc.x = fmaf(wa, c.x, acc.x);
+      acc.y = fmaf(wa, c.y, acc.y);
+      acc.z = fmaf(wa, c.z, acc.z);
+      acc.w += wa;
+    }
+  }
+  rgba[ray] = acc;
+}
+
+// Add g8 (the gradients of one cell's eight corners) to the field gradient,
+// after summing it over the lanes of the warp that carry the same cell.
+__device__ __forceinline__ void flush_cell(float *__restrict__ gfield, const DiffGrid &g,
+                                           int64_t base, const float g8[8], bool active)
+{
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const unsigned peers = __match_any_sync(act, (unsigned long long)base);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  float s[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) s[m] = g8[m];
+  // sum over the other peers (their values fetched one by one)
+  unsigned rest = peers & ~(1u << leader);
+  while (rest) {
+    const int src = __ffs(rest) - 1;
+    rest &= rest - 1;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const float x = __shfl_sync(peers, g8[m], src);
+      if (lane == leader) s[m] += x;
+    }
+  }
+  if (lane != leader) return;
+  const int64_t sy = g.dims[0], sz = (int64_t)g.dims[0] * g.dims[1];
+  const int64_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+#pragma unroll
+  for (int m = 0; m < 8; ++m)
+    if (s[m] != 0.f) atomicAdd(gfield + base + off[m], s[m]);
+}
+
+__global__ void __launch_bounds__(256)
+diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews views,
+              const DiffParams p, const float4 *__restrict__ g_lut,
+              const float4 *__restrict__ grad_rgba, const float4 *__restrict__ ckpt,
+              float *__restrict__ gfield, float *__restrict__ glut)
+{
+  extern __shared__ float4 smem[];
+  float4 *lut = smem;
+  float *slg = reinterpret_cast<float *>(smem + p.lut_size);  // LUT gradient, 4 * lut_size
+  for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) {
+    lut[i] = g_lut[i];
+    slg[4 * i] = slg[4 * i + 1] = slg[4 * i + 2] = slg[4 * i + 3] = 0.f;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  const int py = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+  const int v = blockIdx.z;
+  const bool inside = px < p.width && py < p.height;
+  float o[3], d[3], t0 = 0.f, t1 = 0.f;
+  const bool hit = inside && diff_ray(views.v[v], g, p, min(px, p.width - 1), min(py, p.height - 1),
+                                      o, d, t0, t1);
+  int n = 0;
+  float4 gr = make_float4(0.f, 0.f, 0.f, 0.f);
+  float A[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f};
+  int64_t ray = 0;
+  if (hit) {
+    ray = ((int64_t)v * p.height + py) * p.width + px;
+    gr = grad_rgba[ray];
+    for (int a = 0; a < 3; ++a) {
+      A[a] = (o[a] - g.origin[a]) * g.inv_spacing[a];
+      B[a] = d[a] * g.inv_spacing[a];
+    }
+    while (fmaf((float)n, p.sample_dist, t0) < t1) ++n;
+  }
+  // the warp walks segments in lock step so that lanes can pool their
+  // field gradients; lanes with fewer segments idle
+  int nseg = hit ? (n + kDiffK - 1) / kDiffK : 0;
+  int max_seg = nseg;
+  for (int off = 16; off > 0; off >>= 1) max_seg = max(max_seg, __shfl_xor_sync(0xffffffffu, max_seg, off));
+  float Rr = 0.f, Rg = 0.f, Rb = 0.f, Ra = 0.f;  // suffix composite behind the sample
+  float T[kDiffK], V[kDiffK];
+  int64_t cur = -1;
+  float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int sidx = max_seg - 1; sidx >= 0; --sidx) {
+    const bool seg_on = sidx < nseg;
+    const int k0 = sidx * kDiffK, k1 = min(k0 + kDiffK, n);
+    // re-march the segment from its checkpoint
+    if (seg_on) {
+      float4 acc = ckpt[ray * p.n_seg + sidx];
+      for (int k = k0; k < k1; ++k) {
+        const float t = fmaf((float)k, p.sample_dist, t0);
+        float w[3];
+        const int64_t base = diff_cell(g, A, B, t, w);
+        const float val = diff_value(field, g, base, w);
+        float s_raw, wl;
+        int i0;
+        const float4 c = diff_lut(lut, p, val, s_raw, i0, wl);
+        T[k - k0] = 1.f - acc.w;
+        V[k - k0] = val;
+        const float wa = (1.f - acc.w) * c.w;
+        acc.x = fmaf(wa, c.x, acc.x);
+        acc.y = fmaf(wa, c.y, acc.y);
+        acc.z = fmaf(wa, c.z, acc.z);
+        acc.w += wa;
+      }
+    }
+    // walk it back to front (uniform trip count across the warp)
+    for (int j = kDiffK - 1; j >= 0; --j) {
+      const int k = k0 + j;
+      const bool on = seg_on && k < k1;
+      int64_t base = -1;
+      float w[3] = {0.f, 0.f, 0.f}, dv = 0.f;
+      if (on) {
+        const float t = fmaf((float)k, p.sample_dist, t0);
+        base = diff_cell(g, A, B, t, w);
+        float s_raw, wl;
+        int i0;
+        const float4 c = diff_lut(lut, p, V[j], s_raw, i0, wl);
+        const float Tk = T[j];
+        const float ta = Tk * c.w;
+        const float dcr = ta * gr.x, dcg = ta * gr.y, dcb = ta * gr.z;
+        const float da = Tk * (gr.x * (c.x - Rr) + gr.y * (c.y - Rg) + gr.z * (c.z - Rb) +
+                               gr.w * (1.f - Ra));
+        Rr = fmaf(c.w, c.x, (1.f - c.w) * Rr);
+        Rg = fmaf(c.w, c.y, (1.f - c.w) * Rg);
+        Rb = fmaf(c.w, c.z, (1.f - c.w) * Rb);
+        Ra = c.w + (1.f - c.w) * Ra;
+        // transfer-function entries i0 and i0 + 1
+        const float w0 = 1.f - wl;
+        atomicAdd(slg + 4 * i0 + 0, w0 * dcr);
+        atomicAdd(slg + 4 * i0 + 1, w0 * dcg);
+        atomicAdd(slg + 4 * i0 + 2, w0 * dcb);
+        atomicAdd(slg + 4 * i0 + 3, w0 * da);
+        atomicAdd(slg + 4 * (i0 + 1) + 0, wl * dcr);
+        atomicAdd(slg + 4 * (i0 + 1) + 1, wl * dcg);
+        atomicAdd(slg + 4 * (i0 + 1) + 2, wl * dcb);
+        atomicAdd(slg + 4 * (i0 + 1) + 3, wl * da);
+        // scalar: d(rgba)/dx = lut[i0 + 1] - lut[i0], x = s (n - 1)
+        if (s_raw > 0.f && s_raw < 1.f) {
+          const float4 a0 = lut[i0], a1 = lut[i0 + 1];
+          const float dx = dcr * (a1.x - a0.x) + dcg * (a1.y - a0.y) + dcb * (a1.z - a0.z) +
+                           da * (a1.w - a0.w);
+          dv = dx * (float)(p.lut_size - 1) * p.inv_range;
+        }
+      }
+      // pool the field gradient per cell; flush when a lane changes cell
+      const bool change = on && base != cur && cur >= 0;
+      if (__any_sync(0xffffffffu, change)) flush_cell(gfield, g, cur, g8, change);
+      if (change) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) g8[m] = 0.f;
+      }
+      if (on) {
+        cur = base;
+        const float x0 = 1.f - w[0], y0 = 1.f - w[1], z0 = 1.f - w[2];
+        g8[0] = fmaf(dv, x0 * y0 * z0, g8[0]);
+        g8[1] = fmaf(dv, w[0] * y0 * z0, g8[1]);
+        g8[2] = fmaf(dv, x0 * w[1] * z0, g8[2]);
+        g8[3] = fmaf(dv, w[0] * w[1] * z0, g8[3]);
+        g8[4] = fmaf(dv, x0 * y0 * w[2], g8[4]);
+        g8[5] = fmaf(dv, w[0] * y0 * w[2], g8[5]);
+        g8[6] = fmaf(dv, x0 * w[1] * w[2], g8[6]);
+        g8[7] = fmaf(dv, w[0] * w[1] * w[2], g8[7]);
+      }
+    }
+  }
+  flush_cell(gfield, g, cur, g8, cur >= 0);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 4 * p.lut_size; i += blockDim.x)
+    if (slg[i] != 0.f) atomicAdd(glut + i, slg[i]);
+}
+
+int diff_setup(const float *field, const int dims[3], const double origin[3],
+               const double spacing[3], const gvr_camera *cameras, int n_views,
+               const gvr_render_params *params, DiffGrid &g, DiffViews &views, DiffParams &p)
+{
+  if (!field || !dims || !origin || !spacing || !cameras || !params)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n_views < 1 || n_views > kMaxDiffViews)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "the differentiable render takes 1..64 views");
+  if (params->width < 1 || params->height < 1 || params->lut_size < 2 || params->lut_size > kDiffLut)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad image size or lut_size (2..4096)");
+  if (!(params->sample_dist > 0)) return set_error(GVR_ERR_INVALID_ARGUMENT, "sample_dist must be > 0");
+  double diag = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (dims[a] < 2 || !(spacing[a] > 0))
+      return set_error(GVR_ERR_INVALID_ARGUMENT, "dims >= 2 and spacing > 0 required");
+    const float o = (float)origin[a], sp = (float)spacing[a];
+    g.dims[a] = dims[a];
+    g.origin[a] = o;
+    g.inv_spacing[a] = 1.f / sp;
+    g.lo[a] = o;
+    g.hi[a] = (float)((double)o + (double)(dims[a] - 1) * sp);
+    diag += (double)(dims[a] - 1) * sp * (double)(dims[a] - 1) * sp;
+  }
+  for (int v = 0; v < n_views; ++v) make_view(cameras[v], params->width, params->height, &views.v[v]);
+  p.width = params->width;
+  p.height = params->height;
+  p.n_views = n_views;
+  p.lut_size = params->lut_size;
+  p.sample_dist = params->sample_dist;
+  p.scalar_min = params->scalar_min;
+  p.inv_range = params->scalar_max > params->scalar_min
+                    ? 1.f / (params->scalar_max - params->scalar_min) : 0.f;
+  const double max_samples = std::sqrt(diag) / params->sample_dist + 2.0;
+  p.n_seg = (int)((max_samples + kDiffK - 1) / kDiffK);
+  return GVR_OK;
+}
+
+}  // namespace
+}  // namespace gvr
+
+using namespace gvr;
+
+extern "C" {
+
+int gvr_diff_checkpoints(const int dims[3], const double spacing[3], float sample_dist,
+                         int *per_ray)
+{
+  if (!dims || !spacing || !per_ray || !(sample_dist > 0))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad arguments");
+  double diag = 0;
+  for (int a = 0; a < 3; ++a) diag += (double)(dims[a] - 1) * spacing[a] * (double)(dims[a] - 1) * spacing[a];
+  const double max_samples = std::sqrt(diag) / sample_dist + 2.0;
+  *per_ray = (int)((max_samples + kDiffK - 1) / kDiffK);
+  return GVR_OK;
+}
+
+int gvr_diff_render_forward(const float *field, const int dims[3], const double origin[3],
+                            const double spacing[3], const gvr_camera *cameras, int n_views,
+                            const gvr_render_params *params, const float *lut, float *rgba,
+                            float *checkpoints, void *stream)
+{
+  DiffGrid g;
+  DiffViews views;
+  DiffParams p;
+  int rc = diff_setup(field, dims, origin, spacing, cameras, n_views, params, g, views, p);
+  if (rc != GVR_OK) return rc;
+  if (!lut || !rgba) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL lut or rgba");
+  const size_t smem = sizeof(float4) * p.lut_size;
+  cudaError_t e = cudaFuncSetAttribute(diff_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(float4) * kDiffLut));
+  if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
+  dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
+  diff_forward<<<grid, 256, smem, (cudaStream_t)stream>>>(field, g, views, p, (const float4 *)lut,
+                                                          (float4 *)rgba, (float4 *)checkpoints);
+  count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "differentiable forward launch");
+  return GVR_OK;
+}
+
+int gvr_diff_render_backward(const float *field, const int dims[3], const double origin[3],
+                             const double spacing[3], const gvr_camera *cameras, int n_views,
+                             const gvr_render_params *params, const float *lut,
+                             const float *grad_rgba, const float *checkpoints, float *grad_field,
+                             float *grad_lut, void *stream)
+{
+  DiffGrid g;
+  DiffViews views;
+  DiffParams p;
+  int rc = diff_setup(field, dims, origin, spacing, cameras, n_views, params, g, views, p);
+  if (rc != GVR_OK) return rc;
+  if (!lut || !grad_rgba || !checkpoints || !grad_field || !grad_lut)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL buffer");
+  const size_t smem = sizeof(float4) * p.lut_size * 2;
+  cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(float4) * kDiffLut * 2));
+  if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
+  dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
+  diff_backward<<<grid, 256, smem, (cudaStream_t)stream>>>(
+      field, g, views, p, (const float4 *)lut, (const float4 *)grad_rgba,
+      (const float4 *)checkpoints, grad_field, grad_lut);
+  count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "differentiable backward launch");
+  return GVR_OK;
+}
+
+}  // extern "C"

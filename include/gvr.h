@@ -294,6 +294,41 @@ GVR_API int gvr_scene_set_batch_granularity(gvr_scene *scene, int tiles_per_item
  * diagnostic; no counterpart in the reference). */
 GVR_API int gvr_scene_batch_graph_builds(const gvr_scene *scene, int *n);
 
+/* ------------------------------------------------------------------ */
+/* Differentiable render (no counterpart in the reference)              */
+/* ------------------------------------------------------------------ */
+
+/* Checkpoint records per ray the differentiable forward writes for a grid
+ * of node dims and spacing at this sample distance (one float4 every 64
+ * samples); the checkpoint buffer holds n_views * W * H * per_ray float4. */
+GVR_API int gvr_diff_checkpoints(const int dims[3], const double spacing[3], float sample_dist,
+                                 int *per_ray);
+
+/* Forward render of one uniform domain for 1..64 views with a linearly
+ * interpolated transfer function and no partial culling, so that the image
+ * is differentiable in the node field and the LUT. field (node values, x
+ * fastest), lut (lut_size RGBA floats), rgba (n_views * W * H * 4) and
+ * checkpoints (may be NULL for an inference-only pass) are device pointers.
+ * Other fields of params used: width, height, sample_dist, scalar range,
+ * lut_size. */
+GVR_API int gvr_diff_render_forward(const float *field, const int dims[3], const double origin[3],
+                                    const double spacing[3], const gvr_camera *cameras,
+                                    int n_views, const gvr_render_params *params,
+                                    const float *lut, float *rgba, float *checkpoints,
+                                    void *stream);
+
+/* Adjoint of gvr_diff_render_forward: given dL/d(rgba) (device, same layout
+ * as rgba) and the forward's checkpoints, ADD dL/d(field) into grad_field
+ * (node layout) and dL/d(lut) into grad_lut (lut_size * 4). Segments of 64
+ * samples are re-marched from their checkpoints; the blend is never
+ * inverted. */
+GVR_API int gvr_diff_render_backward(const float *field, const int dims[3],
+                                     const double origin[3], const double spacing[3],
+                                     const gvr_camera *cameras, int n_views,
+                                     const gvr_render_params *params, const float *lut,
+                                     const float *grad_rgba, const float *checkpoints,
+                                     float *grad_field, float *grad_lut, void *stream);
+
 /* Render one uniform domain without allocating any device memory; no
  * counterpart in the reference. For callers that may not call cudaMalloc or
  * cudaFree — typically a simulation that gives all GPU memory to its own
