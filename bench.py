@@ -286,6 +286,48 @@ def bench_batch(dev, reps=5):
             "graph_captures": builds}
 
 
+def bench_diff(dev, n=128, views=16, size=256, reps=5):
+    """Differentiable render: n^3 field, 256-entry LUT, `views` Cinema views at
+    size^2; L2 loss against images of the field + N(0, 0.05) (seed 5)."""
+    import torch
+    from ascent_gb300 import diff as D
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import workloads as W
+    wl = W.plain_small(n=n, width=size, height=size, seed=5)
+    d = wl.domains[0]
+    side = int(round(views ** 0.5))
+    cams = S.cinema_cameras(wl.bounds, W.cinema_angles(side, views // side))
+    x = np.linspace(0, 1, 256)
+    lut = torch.from_numpy(np.stack([x, np.full_like(x, 0.5), 1 - x, 0.3 * x], 1).astype(np.float32)).cuda(dev)
+    sd = S.sample_distance(wl.bounds, int(np.ceil(np.sqrt(3) * (n - 1) / 0.5)))
+    rng = np.random.default_rng(5)
+    gt = torch.from_numpy(d.field).cuda(dev)
+    with torch.no_grad():
+        pert = gt + torch.from_numpy(rng.normal(0, 0.05, d.field.shape).astype(np.float32)).cuda(dev)
+        target = D.render(pert, lut, cams, d.origin, d.spacing, size, size, sd, wl.scalar_range)
+    f = gt.clone().requires_grad_(True)
+    lt = lut.clone().requires_grad_(True)
+    stream = torch.cuda.current_stream(dev)
+
+    def fwd():
+        with torch.no_grad():
+            return D.render(f, lt, cams, d.origin, d.spacing, size, size, sd, wl.scalar_range)
+
+    def fwd_bwd():
+        f.grad = None
+        lt.grad = None
+        img = D.render(f, lt, cams, d.origin, d.spacing, size, size, sd, wl.scalar_range)
+        ((img - target) ** 2).sum().backward()
+
+    for _ in range(2):
+        fwd_bwd()
+    fwd_ms = _timed(fwd, stream, reps)
+    fb_ms = _timed(fwd_bwd, stream, reps)
+    return {"workload": f"diff{n}^3x{views}views@{size}x{size}", "lut": 256, "checkpoint_every": 64,
+            "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "fwd_bwd_over_fwd": fb_ms / fwd_ms,
+            "grad_field_norm": float(f.grad.norm()), "grad_lut_norm": float(lt.grad.norm())}
+
+
 def run_reference(args):
     """CPU implementation of the path (the oracle's FP32 OpenMP port) on this host."""
     rank = int(os.environ.get("RANK", "0"))
@@ -443,6 +485,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         others["hex"] = bench_hex(dev)
         others["batched"] = bench_batch(dev)
+        others["differentiable"] = bench_diff(dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
