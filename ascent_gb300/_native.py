@@ -130,8 +130,8 @@ _SIGS = {
     "gvr_scene_update_field": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int64, C.c_int]),
     "gvr_scene_num_domains": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "gvr_scene_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
-    "gvr_diff_checkpoints": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_float,
-                                       C.POINTER(C.c_int)]),
+    "gvr_diff_workspace": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_float,
+                                     C.POINTER(C.c_int)]),
     "gvr_diff_render_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                           C.POINTER(C.c_double), C.c_void_p, C.c_int,
                                           C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p,

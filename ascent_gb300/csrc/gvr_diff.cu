@@ -9,20 +9,24 @@
 // field in its plain layout (x fastest) and the LUT (n RGBA floats), both
 // differentiable.
 //
-// Forward: one thread per ray; every kDiffK samples it stores the
-// accumulated (rgb, alpha) at the start of the segment.
-// Backward: per ray, segments from last to first. A segment is re-marched
-// from its checkpoint, keeping each sample's transmittance T_k and scalar v_k
-// in thread-local arrays (the blend is never inverted); then its samples are
-// walked back to front with the suffix composite (R', A') of the samples
-// behind them:
+// Forward (training): one thread per ray; it stores the transmittance at the
+// start of every kDiffK-sample segment and caches every sample's scalar v_k
+// in a workspace ([sample][ray], so that a warp writes contiguous rays).
+// Backward: per ray, segments from last to first. A segment's transmittances
+// T_k are rebuilt forward from its checkpoint through the cached scalars and
+// the LUT — no field loads, and the blend is never inverted — into a
+// thread-local array; then its samples are walked back to front with the
+// suffix composite (R', A') of the samples behind them:
 //   dL/dc_k = T_k a_k g_rgb,
 //   dL/da_k = T_k (g_rgb . (c_k - R'_k) + g_A (1 - A'_k)),
 //   R'_{k-1} = a_k c_k + (1 - a_k) R'_k,  A'_{k-1} = a_k + (1 - a_k) A'_k.
-// LUT gradients accumulate in shared memory per CTA; field gradients are
+// LUT gradients accumulate in up to 16 private shared-memory copies per CTA
+// (lane l uses copy l % 16, so neighbouring rays that hit the same entry do
+// not serialise on one address), summed once per CTA; field gradients are
 // summed per ray while consecutive samples stay in one cell, then combined
 // across the lanes of a warp that hit the same cell (__match_any_sync) and
 // added to the eight corners with one atomic per distinct node.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -53,7 +57,10 @@ struct DiffParams {
   int height;
   int n_views;
   int lut_size;
-  int n_seg;
+  int lut_copies;  // private LUT-gradient copies per CTA (backward)
+  int n_seg;       // checkpoint segments per ray
+  int64_t n_rays;  // views x height x width
+  int64_t v_offset;  // start of the per-sample scalar cache in the workspace
   float sample_dist;
   float scalar_min;
   float inv_range;
@@ -135,7 +142,7 @@ __device__ __forceinline__ float4 diff_lut(const float4 *lut, const DiffParams &
 __global__ void __launch_bounds__(256)
 diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews views,
              const DiffParams p, const float4 *__restrict__ g_lut, float4 *__restrict__ rgba,
-             float4 *__restrict__ ckpt)
+             float *__restrict__ ws)
 {
   extern __shared__ float4 lut[];
   for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) lut[i] = g_lut[i];
@@ -157,10 +164,14 @@ diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews 
     for (int k = 0;; ++k) {
       const float t = fmaf((float)k, p.sample_dist, t0);
       if (!(t < t1)) break;
-      if (ckpt && (k % kDiffK) == 0 && k / kDiffK < p.n_seg) ckpt[ray * p.n_seg + k / kDiffK] = acc;
+      if (ws) {
+        // transmittance checkpoint at each segment start, scalar of every sample
+        if ((k % kDiffK) == 0) ws[ray * p.n_seg + k / kDiffK] = 1.f - acc.w;
+      }
       float w[3];
       const int64_t base = diff_cell(g, A, B, t, w);
       const float val = diff_value(field, g, base, w);
+      if (ws) ws[p.v_offset + (int64_t)k * p.n_rays + ray] = val;
       float s_raw, wl;
       int i0;
       const float4 c = diff_lut(lut, p, val, s_raw, i0, wl);
@@ -209,16 +220,19 @@ __device__ __forceinline__ void flush_cell(float *__restrict__ gfield, const Dif
 __global__ void __launch_bounds__(256)
 diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews views,
               const DiffParams p, const float4 *__restrict__ g_lut,
-              const float4 *__restrict__ grad_rgba, const float4 *__restrict__ ckpt,
+              const float4 *__restrict__ grad_rgba, const float *__restrict__ ws,
               float *__restrict__ gfield, float *__restrict__ glut)
 {
   extern __shared__ float4 smem[];
   float4 *lut = smem;
-  float *slg = reinterpret_cast<float *>(smem + p.lut_size);  // LUT gradient, 4 * lut_size
-  for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) {
-    lut[i] = g_lut[i];
-    slg[4 * i] = slg[4 * i + 1] = slg[4 * i + 2] = slg[4 * i + 3] = 0.f;
-  }
+  // LUT gradient: p.lut_copies private copies of 4 * lut_size floats, one
+  // float of padding apart so that equal entries of different copies sit in
+  // different banks; lane l adds into copy l % lut_copies, so the lanes of a
+  // warp that hit the same entry mostly hit different addresses
+  float *slg = reinterpret_cast<float *>(smem + p.lut_size);
+  const int cstride = 4 * p.lut_size + 1;
+  for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) lut[i] = g_lut[i];
+  for (int i = threadIdx.x; i < cstride * p.lut_copies; i += blockDim.x) slg[i] = 0.f;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -247,30 +261,23 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
   int max_seg = nseg;
   for (int off = 16; off > 0; off >>= 1) max_seg = max(max_seg, __shfl_xor_sync(0xffffffffu, max_seg, off));
   float Rr = 0.f, Rg = 0.f, Rb = 0.f, Ra = 0.f;  // suffix composite behind the sample
-  float T[kDiffK], V[kDiffK];
+  float T[kDiffK];
   int64_t cur = -1;
   float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int sidx = max_seg - 1; sidx >= 0; --sidx) {
     const bool seg_on = sidx < nseg;
     const int k0 = sidx * kDiffK, k1 = min(k0 + kDiffK, n);
-    // re-march the segment from its checkpoint
+    // transmittance of every sample of the segment, forward from its
+    // checkpoint through the cached scalars (no field loads)
     if (seg_on) {
-      float4 acc = ckpt[ray * p.n_seg + sidx];
+      float Tr = ws[ray * p.n_seg + sidx];
       for (int k = k0; k < k1; ++k) {
-        const float t = fmaf((float)k, p.sample_dist, t0);
-        float w[3];
-        const int64_t base = diff_cell(g, A, B, t, w);
-        const float val = diff_value(field, g, base, w);
+        const float val = ws[p.v_offset + (int64_t)k * p.n_rays + ray];
         float s_raw, wl;
         int i0;
         const float4 c = diff_lut(lut, p, val, s_raw, i0, wl);
-        T[k - k0] = 1.f - acc.w;
-        V[k - k0] = val;
-        const float wa = (1.f - acc.w) * c.w;
-        acc.x = fmaf(wa, c.x, acc.x);
-        acc.y = fmaf(wa, c.y, acc.y);
-        acc.z = fmaf(wa, c.z, acc.z);
-        acc.w += wa;
+        T[k - k0] = Tr;
+        Tr *= 1.f - c.w;
       }
     }
     // walk it back to front (uniform trip count across the warp)
@@ -284,7 +291,7 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
         base = diff_cell(g, A, B, t, w);
         float s_raw, wl;
         int i0;
-        const float4 c = diff_lut(lut, p, V[j], s_raw, i0, wl);
+        const float4 c = diff_lut(lut, p, ws[p.v_offset + (int64_t)k * p.n_rays + ray], s_raw, i0, wl);
         const float Tk = T[j];
         const float ta = Tk * c.w;
         const float dcr = ta * gr.x, dcg = ta * gr.y, dcb = ta * gr.z;
@@ -296,14 +303,15 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
         Ra = c.w + (1.f - c.w) * Ra;
         // transfer-function entries i0 and i0 + 1
         const float w0 = 1.f - wl;
-        atomicAdd(slg + 4 * i0 + 0, w0 * dcr);
-        atomicAdd(slg + 4 * i0 + 1, w0 * dcg);
-        atomicAdd(slg + 4 * i0 + 2, w0 * dcb);
-        atomicAdd(slg + 4 * i0 + 3, w0 * da);
-        atomicAdd(slg + 4 * (i0 + 1) + 0, wl * dcr);
-        atomicAdd(slg + 4 * (i0 + 1) + 1, wl * dcg);
-        atomicAdd(slg + 4 * (i0 + 1) + 2, wl * dcb);
-        atomicAdd(slg + 4 * (i0 + 1) + 3, wl * da);
+        float *q = slg + (lane % p.lut_copies) * cstride + 4 * i0;
+        atomicAdd(q + 0, w0 * dcr);
+        atomicAdd(q + 1, w0 * dcg);
+        atomicAdd(q + 2, w0 * dcb);
+        atomicAdd(q + 3, w0 * da);
+        atomicAdd(q + 4, wl * dcr);
+        atomicAdd(q + 5, wl * dcg);
+        atomicAdd(q + 6, wl * dcb);
+        atomicAdd(q + 7, wl * da);
         // scalar: d(rgba)/dx = lut[i0 + 1] - lut[i0], x = s (n - 1)
         if (s_raw > 0.f && s_raw < 1.f) {
           const float4 a0 = lut[i0], a1 = lut[i0 + 1];
@@ -336,7 +344,11 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
   flush_cell(gfield, g, cur, g8, cur >= 0);
   __syncthreads();
   for (int i = threadIdx.x; i < 4 * p.lut_size; i += blockDim.x)
-    if (slg[i] != 0.f) atomicAdd(glut + i, slg[i]);
+  {
+    float acc = 0.f;
+    for (int c = 0; c < p.lut_copies; ++c) acc += slg[c * cstride + i];
+    if (acc != 0.f) atomicAdd(glut + i, acc);
+  }
 }
 
 int diff_setup(const float *field, const int dims[3], const double origin[3],
@@ -367,12 +379,15 @@ int diff_setup(const float *field, const int dims[3], const double origin[3],
   p.height = params->height;
   p.n_views = n_views;
   p.lut_size = params->lut_size;
+  p.lut_copies = 1;
   p.sample_dist = params->sample_dist;
   p.scalar_min = params->scalar_min;
   p.inv_range = params->scalar_max > params->scalar_min
                     ? 1.f / (params->scalar_max - params->scalar_min) : 0.f;
   const double max_samples = std::sqrt(diag) / params->sample_dist + 2.0;
   p.n_seg = (int)((max_samples + kDiffK - 1) / kDiffK);
+  p.n_rays = (int64_t)n_views * params->width * params->height;
+  p.v_offset = p.n_rays * p.n_seg;
   return GVR_OK;
 }
 
@@ -383,22 +398,23 @@ using namespace gvr;
 
 extern "C" {
 
-int gvr_diff_checkpoints(const int dims[3], const double spacing[3], float sample_dist,
-                         int *per_ray)
+int gvr_diff_workspace(const int dims[3], const double spacing[3], float sample_dist,
+                       int *floats_per_ray)
 {
-  if (!dims || !spacing || !per_ray || !(sample_dist > 0))
+  if (!dims || !spacing || !floats_per_ray || !(sample_dist > 0))
     return set_error(GVR_ERR_INVALID_ARGUMENT, "bad arguments");
   double diag = 0;
   for (int a = 0; a < 3; ++a) diag += (double)(dims[a] - 1) * spacing[a] * (double)(dims[a] - 1) * spacing[a];
   const double max_samples = std::sqrt(diag) / sample_dist + 2.0;
-  *per_ray = (int)((max_samples + kDiffK - 1) / kDiffK);
+  const int n_seg = (int)((max_samples + kDiffK - 1) / kDiffK);
+  *floats_per_ray = n_seg * (1 + kDiffK);
   return GVR_OK;
 }
 
 int gvr_diff_render_forward(const float *field, const int dims[3], const double origin[3],
                             const double spacing[3], const gvr_camera *cameras, int n_views,
                             const gvr_render_params *params, const float *lut, float *rgba,
-                            float *checkpoints, void *stream)
+                            float *workspace, void *stream)
 {
   DiffGrid g;
   DiffViews views;
@@ -412,7 +428,7 @@ int gvr_diff_render_forward(const float *field, const int dims[3], const double 
   if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
   dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
   diff_forward<<<grid, 256, smem, (cudaStream_t)stream>>>(field, g, views, p, (const float4 *)lut,
-                                                          (float4 *)rgba, (float4 *)checkpoints);
+                                                          (float4 *)rgba, workspace);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "differentiable forward launch");
@@ -422,7 +438,7 @@ int gvr_diff_render_forward(const float *field, const int dims[3], const double 
 int gvr_diff_render_backward(const float *field, const int dims[3], const double origin[3],
                              const double spacing[3], const gvr_camera *cameras, int n_views,
                              const gvr_render_params *params, const float *lut,
-                             const float *grad_rgba, const float *checkpoints, float *grad_field,
+                             const float *grad_rgba, const float *workspace, float *grad_field,
                              float *grad_lut, void *stream)
 {
   DiffGrid g;
@@ -430,16 +446,19 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   DiffParams p;
   int rc = diff_setup(field, dims, origin, spacing, cameras, n_views, params, g, views, p);
   if (rc != GVR_OK) return rc;
-  if (!lut || !grad_rgba || !checkpoints || !grad_field || !grad_lut)
+  if (!lut || !grad_rgba || !workspace || !grad_field || !grad_lut)
     return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL buffer");
-  const size_t smem = sizeof(float4) * p.lut_size * 2;
+  // up to 16 private LUT-gradient copies within ~72 KB of shared memory
+  const size_t per_copy = sizeof(float) * (4 * (size_t)p.lut_size + 1);
+  p.lut_copies = (int)std::max<size_t>(1, std::min<size_t>(16, (72u << 10) / per_copy));
+  const size_t smem = sizeof(float4) * p.lut_size + per_copy * p.lut_copies;
   cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(sizeof(float4) * kDiffLut * 2));
+                                       (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
   dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
   diff_backward<<<grid, 256, smem, (cudaStream_t)stream>>>(
       field, g, views, p, (const float4 *)lut, (const float4 *)grad_rgba,
-      (const float4 *)checkpoints, grad_field, grad_lut);
+      workspace, grad_field, grad_lut);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "differentiable backward launch");

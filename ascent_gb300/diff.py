@@ -25,10 +25,12 @@ def _geom(field: torch.Tensor, origin, spacing):
     return dims, o, s
 
 
-def checkpoints_per_ray(field_shape, spacing, sample_dist: float) -> int:
+def workspace_per_ray(field_shape, spacing, sample_dist: float) -> int:
+    """Floats per ray of the training workspace (transmittance checkpoints
+    every 64 samples + the scalar of every sample)."""
     nz, ny, nx = field_shape
     n = C.c_int()
-    N.call("gvr_diff_checkpoints", (C.c_int * 3)(nx, ny, nz), (C.c_double * 3)(*map(float, spacing)),
+    N.call("gvr_diff_workspace", (C.c_int * 3)(nx, ny, nz), (C.c_double * 3)(*map(float, spacing)),
            float(sample_dist), C.byref(n))
     return n.value
 
@@ -48,13 +50,15 @@ class VolumeRender(torch.autograd.Function):
         v, h, w = len(cameras), params.height, params.width
         cams = (N.Camera * v)(*cameras)
         dims, o, s = _geom(field, origin, spacing)
-        per_ray = checkpoints_per_ray(field.shape, spacing, params.sample_dist)
+        per_ray = workspace_per_ray(field.shape, spacing, params.sample_dist)
         rgba = torch.empty((v, h, w, 4), dtype=torch.float32, device=field.device)
-        ckpt = torch.empty((v * h * w * per_ray, 4), dtype=torch.float32, device=field.device)
+        need_ws = bool(ctx.needs_input_grad[0] or ctx.needs_input_grad[1])
+        ckpt = torch.empty((v * h * w * per_ray if need_ws else 1,), dtype=torch.float32,
+                           device=field.device)
         stream = C.c_void_p(torch.cuda.current_stream(field.device).cuda_stream)
         N.call("gvr_diff_render_forward", C.c_void_p(field.data_ptr()), dims, o, s, cams, v,
                C.byref(params), C.c_void_p(lut.data_ptr()), C.c_void_p(rgba.data_ptr()),
-               C.c_void_p(ckpt.data_ptr()), stream)
+               C.c_void_p(ckpt.data_ptr()) if need_ws else None, stream)
         ctx.save_for_backward(field, lut, ckpt)
         ctx.cams = cams
         ctx.geom = (origin, spacing)

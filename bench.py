@@ -319,12 +319,19 @@ def bench_diff(dev, n=128, views=16, size=256, reps=5):
         img = D.render(f, lt, cams, d.origin, d.spacing, size, size, sd, wl.scalar_range)
         ((img - target) ** 2).sum().backward()
 
+    def fwd_train():
+        return D.render(f, lt, cams, d.origin, d.spacing, size, size, sd, wl.scalar_range)
+
     for _ in range(2):
         fwd_bwd()
     fwd_ms = _timed(fwd, stream, reps)
+    train_ms = _timed(fwd_train, stream, reps)
     fb_ms = _timed(fwd_bwd, stream, reps)
     return {"workload": f"diff{n}^3x{views}views@{size}x{size}", "lut": 256, "checkpoint_every": 64,
-            "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "fwd_bwd_over_fwd": fb_ms / fwd_ms,
+            "fwd_ms": fwd_ms, "fwd_train_ms": train_ms, "fwd_bwd_ms": fb_ms,
+            "fwd_bwd_over_fwd": fb_ms / fwd_ms,
+            "note": "fwd = inference forward (no workspace); fwd_bwd = training forward "
+                    "(checkpoints + per-sample scalars) + L2 loss + adjoint",
             "grad_field_norm": float(f.grad.norm()), "grad_lut_norm": float(lt.grad.norm())}
 
 

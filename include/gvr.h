@@ -298,11 +298,12 @@ GVR_API int gvr_scene_batch_graph_builds(const gvr_scene *scene, int *n);
 /* Differentiable render (no counterpart in the reference)              */
 /* ------------------------------------------------------------------ */
 
-/* Checkpoint records per ray the differentiable forward writes for a grid
- * of node dims and spacing at this sample distance (one float4 every 64
- * samples); the checkpoint buffer holds n_views * W * H * per_ray float4. */
-GVR_API int gvr_diff_checkpoints(const int dims[3], const double spacing[3], float sample_dist,
-                                 int *per_ray);
+/* Floats per ray of the training workspace the differentiable forward
+ * fills for a grid of node dims and spacing at this sample distance: one
+ * transmittance checkpoint every 64 samples plus the scalar of every sample.
+ * The workspace holds n_views * W * H * floats_per_ray floats. */
+GVR_API int gvr_diff_workspace(const int dims[3], const double spacing[3], float sample_dist,
+                               int *floats_per_ray);
 
 /* Forward render of one uniform domain for 1..64 views with a linearly
  * interpolated transfer function and no partial culling, so that the image
@@ -314,19 +315,19 @@ GVR_API int gvr_diff_checkpoints(const int dims[3], const double spacing[3], flo
 GVR_API int gvr_diff_render_forward(const float *field, const int dims[3], const double origin[3],
                                     const double spacing[3], const gvr_camera *cameras,
                                     int n_views, const gvr_render_params *params,
-                                    const float *lut, float *rgba, float *checkpoints,
+                                    const float *lut, float *rgba, float *workspace,
                                     void *stream);
 
 /* Adjoint of gvr_diff_render_forward: given dL/d(rgba) (device, same layout
- * as rgba) and the forward's checkpoints, ADD dL/d(field) into grad_field
- * (node layout) and dL/d(lut) into grad_lut (lut_size * 4). Segments of 64
- * samples are re-marched from their checkpoints; the blend is never
- * inverted. */
+ * as rgba) and the forward's workspace, ADD dL/d(field) into grad_field
+ * (node layout) and dL/d(lut) into grad_lut (lut_size * 4). The
+ * transmittances of each 64-sample segment are rebuilt from its checkpoint;
+ * the blend is never inverted. */
 GVR_API int gvr_diff_render_backward(const float *field, const int dims[3],
                                      const double origin[3], const double spacing[3],
                                      const gvr_camera *cameras, int n_views,
                                      const gvr_render_params *params, const float *lut,
-                                     const float *grad_rgba, const float *checkpoints,
+                                     const float *grad_rgba, const float *workspace,
                                      float *grad_field, float *grad_lut, void *stream);
 
 /* Render one uniform domain without allocating any device memory; no
