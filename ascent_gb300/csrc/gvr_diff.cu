@@ -229,9 +229,13 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
   // float of padding apart so that equal entries of different copies sit in
   // different banks; lane l adds into copy l % lut_copies, so the lanes of a
   // warp that hit the same entry mostly hit different addresses
-  float *slg = reinterpret_cast<float *>(smem + p.lut_size);
+  float *lut_a = reinterpret_cast<float *>(smem + p.lut_size);  // opacity column
+  float *slg = lut_a + p.lut_size;
   const int cstride = 4 * p.lut_size + 1;
-  for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) lut[i] = g_lut[i];
+  for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) {
+    lut[i] = g_lut[i];
+    lut_a[i] = g_lut[i].w;
+  }
   for (int i = threadIdx.x; i < cstride * p.lut_copies; i += blockDim.x) slg[i] = 0.f;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -271,13 +275,14 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
     // checkpoint through the cached scalars (no field loads)
     if (seg_on) {
       float Tr = ws[ray * p.n_seg + sidx];
+      const float nm1 = (float)(p.lut_size - 1);
       for (int k = k0; k < k1; ++k) {
         const float val = ws[p.v_offset + (int64_t)k * p.n_rays + ray];
-        float s_raw, wl;
-        int i0;
-        const float4 c = diff_lut(lut, p, val, s_raw, i0, wl);
+        const float x = __saturatef((val - p.scalar_min) * p.inv_range) * nm1;
+        const int i0 = min((int)x, p.lut_size - 2);
+        const float a = lerp2(lut_a[i0], lut_a[i0 + 1], x - (float)i0);
         T[k - k0] = Tr;
-        Tr *= 1.f - c.w;
+        Tr *= 1.f - a;
       }
     }
     // walk it back to front (uniform trip count across the warp)
@@ -451,7 +456,7 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   // up to 16 private LUT-gradient copies within ~72 KB of shared memory
   const size_t per_copy = sizeof(float) * (4 * (size_t)p.lut_size + 1);
   p.lut_copies = (int)std::max<size_t>(1, std::min<size_t>(16, (72u << 10) / per_copy));
-  const size_t smem = sizeof(float4) * p.lut_size + per_copy * p.lut_copies;
+  const size_t smem = (sizeof(float4) + sizeof(float)) * p.lut_size + per_copy * p.lut_copies;
   cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
