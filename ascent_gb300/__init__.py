@@ -9,3 +9,7 @@ Layers:
 from ._native import GvrError, Camera, RenderParams  # noqa: F401
 
 __all__ = ["GvrError", "Camera", "RenderParams"]
+
+from .ascent import Ascent, AscentError  # noqa: E402,F401
+
+__all__ += ["Ascent", "AscentError"]

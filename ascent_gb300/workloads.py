@@ -275,3 +275,29 @@ def plain_large(n_cells: int = 512, seed: int = 2, width: int = 1024, height: in
     rp, rgb, ap, al = linear_ramp_tf()
     return Workload(f"uniform{n_cells}^3x{len(doms)}dom@{width}x{height}", doms, width, height,
                     samples, 30.0, 20.0, rp, rgb, ap, al)
+
+
+def to_blueprint(wl, field: str = "braid") -> list:
+    """The workload's domains as Blueprint-shaped dicts (uniform or explicit hex)."""
+    out = []
+    for i, d in enumerate(wl.domains):
+        if isinstance(d, HexDomain):
+            out.append({
+                "state": {"domain_id": i, "cycle": 100, "time": 1.5},
+                "coordsets": {"coords": {"type": "explicit", "values": {"x": d.x, "y": d.y, "z": d.z}}},
+                "topologies": {"mesh": {"type": "unstructured", "coordset": "coords",
+                                        "elements": {"shape": "hex", "connectivity": d.conn.ravel()}}},
+                "fields": {field: {"association": "vertex", "topology": "mesh", "values": d.field}},
+            })
+        else:
+            nx, ny, nz = d.dims
+            out.append({
+                "state": {"domain_id": i, "cycle": 100, "time": 1.5},
+                "coordsets": {"coords": {"type": "uniform", "dims": {"i": nx, "j": ny, "k": nz},
+                                         "origin": {"x": d.origin[0], "y": d.origin[1], "z": d.origin[2]},
+                                         "spacing": {"dx": d.spacing[0], "dy": d.spacing[1],
+                                                     "dz": d.spacing[2]}}},
+                "topologies": {"mesh": {"type": "uniform", "coordset": "coords"}},
+                "fields": {field: {"association": "vertex", "topology": "mesh", "values": d.field.ravel()}},
+            })
+    return out
