@@ -99,7 +99,8 @@ def test_hex_and_republish(tmp_path):
     a.execute(actions({"r": render}))
     first = decode_png(open(a.info()["images"][0]["image_name"], "rb").read())
     assert first[..., 3].max() > 0
-    bp[0]["fields"]["braid"]["values"] = bp[0]["fields"]["braid"]["values"] * 0.25
+    # a non-linear change (a linear one would be undone by the range normalisation)
+    bp[0]["fields"]["braid"]["values"] = np.sqrt(np.abs(bp[0]["fields"]["braid"]["values"]))
     a.publish(bp)  # same mesh: fields are swapped in place
     a.execute(actions({"r": render}))
     second = decode_png(open(a.info()["images"][0]["image_name"], "rb").read())
