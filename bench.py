@@ -229,7 +229,9 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
     pk = peaks()
     alg = n * 160 + size * size * BYTES_PER_PIXEL
     sc.close()
+    acc = accuracy(dev, wl, [cam], p, rows=(size // 2 - 8, size // 2 + 8))
     return {"workload": wl.name, "cells": n_cells ** 3, "samples_per_frame": n,
+            "error_vs_fp64_oracle": acc,
             "gsamples_per_s": n / ms / 1e6, "fps": 1e3 / ms, "ms_per_frame": ms,
             "bvh_build_ms": build_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
             "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": pk["hbm_gbs"],
@@ -278,11 +280,13 @@ def bench_batch(dev, reps=5):
     same = bool(torch.equal(ref, out[0]))
     builds = sc.batch_graph_builds
     sc.close()
+    acc = accuracy(dev, wl, [cams[0], cams[27]], p, rows=(h // 2 - 32, h // 2 + 32))
     return {"workload": wl.name, "domains": len(wl.domains), "views": v, "image": [w, h],
             "samples_per_batch": n, "per_view_loop_ms": loop_ms, "batched_ms": batch_ms,
             "per_view_loop_images_per_s": v * 1e3 / loop_ms, "batched_images_per_s": v * 1e3 / batch_ms,
             "speedup": loop_ms / batch_ms, "batched_gsamples_per_s": n / batch_ms / 1e6,
             "images_identical_to_loop": same, "loop_tuning": single, "batch_tuning": best["best"],
+            "error_vs_fp64_oracle": acc,
             "graph_captures": builds}
 
 
@@ -327,12 +331,96 @@ def bench_diff(dev, n=128, views=16, size=256, reps=5):
     fwd_ms = _timed(fwd, stream, reps)
     train_ms = _timed(fwd_train, stream, reps)
     fb_ms = _timed(fwd_bwd, stream, reps)
+    from ascent_gb300 import _native as N
+    from oracle import oracle as O
+    p = N.make_params(size, size, sd, wl.scalar_range, lut.cpu().numpy(), lut_filter=N.LUT_LINEAR,
+                      alpha_cull=0.0, early_term=1.0)
+    osc = O.OracleScene(64)
+    osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    with torch.no_grad():
+        img = D.render(gt, lut, cams[:2], d.origin, d.spacing, size, size, sd, wl.scalar_range).cpu().numpy()
+    errs = [_err(img[i], osc.render(cams[i], p)[0]) for i in range(2)]
+    acc = {k: max(e[k] for e in errs) if k != "frac_within_2_255" else min(e[k] for e in errs)
+           for k in errs[0]}
+    acc.update({"views": 2, "oracle": "FP64 CPU oracle (oracle/gvr_oracle.c), linear LUT, no cull"})
     return {"workload": f"diff{n}^3x{views}views@{size}x{size}", "lut": 256, "checkpoint_every": 64,
+            "error_vs_fp64_oracle": acc,
             "fwd_ms": fwd_ms, "fwd_train_ms": train_ms, "fwd_bwd_ms": fb_ms,
             "fwd_bwd_over_fwd": fb_ms / fwd_ms,
             "note": "fwd = inference forward (no workspace); fwd_bwd = training forward "
                     "(checkpoints + per-sample scalars) + L2 loss + adjoint",
             "grad_field_norm": float(f.grad.norm()), "grad_lut_norm": float(lt.grad.norm())}
+
+
+def _err(g, o) -> dict:
+    d = np.abs(g.astype(np.float64) - o.astype(np.float64))
+    return {"max": float(d.max()), "mae": float(d.mean()),
+            "frac_within_2_255": float((d <= 2 / 255 + 1e-7).all(axis=-1).mean()),
+            "frac_over_4_255": float((d > 4 / 255).any(axis=-1).mean())}
+
+
+def accuracy(dev, wl, cams, params, rows=None, precision=64) -> dict:
+    """Error of the GPU images against the FP64 oracle on the same inputs,
+    over image rows [rows[0], rows[1]) (the whole image when None)."""
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import volume as V
+    from oracle import oracle as O
+    osc = O.OracleScene(precision)
+    for d in wl.domains:
+        if hasattr(d, "conn"):
+            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
+        else:
+            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    h, w = params.height, params.width
+    r0, r1 = rows if rows else (0, h)
+    out = []
+    with S.Scene(dev) as sc:
+        V.load_workload(sc, wl)
+        for cam in cams:
+            g, _ = sc.render(cam, params)
+            o = np.zeros((h, w, 4), np.float32)
+            dep = np.zeros((h, w), np.float32)
+            t0 = time.perf_counter()
+            osc.render_rows(cam, params, r0, r1, o, dep)
+            e = _err(g[r0:r1], o[r0:r1])
+            e["oracle_s"] = round(time.perf_counter() - t0, 2)
+            out.append(e)
+    worst = {k: (max if k in ("max", "mae", "frac_over_4_255") else min)(e[k] for e in out)
+             for k in ("max", "mae", "frac_within_2_255", "frac_over_4_255")}
+    worst["rows"] = [r0, r1]
+    worst["views"] = len(cams)
+    worst["oracle"] = "FP64 CPU oracle (oracle/gvr_oracle.c)"
+    return worst
+
+
+def bench_plain_small(dev, reps=20) -> dict:
+    """The CPU-runnable plain case: one 64^3 field, 512^2, 218 samples,
+    single-domain path (float LUT, uint8 canvas round trip)."""
+    import ctypes as C
+    import torch
+    from ascent_gb300 import _native as N
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import volume as V
+    from ascent_gb300 import workloads as W
+    wl = W.plain_small()
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    stream = torch.cuda.current_stream(dev)
+    with S.Scene(dev) as sc:
+        V.load_workload(sc, wl)
+        rgba = torch.empty((512, 512, 4), dtype=torch.float32, device=f"cuda:{dev}")
+        depth = torch.empty((512, 512), dtype=torch.float32, device=f"cuda:{dev}")
+        _, _, n = sc.render(cam, p, device_out=True, count_samples=True)
+        args = (sc.handle, C.byref(cam), C.byref(p), C.c_void_p(rgba.data_ptr()),
+                C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, C.c_void_p(stream.cuda_stream), None)
+        for _ in range(3):
+            N.call("gvr_render_volume", *args)
+        ms = _timed(lambda: N.call("gvr_render_volume", *args), stream, reps)
+    cpu, _ = cpu_sample(wl, cam, p, 3.0)
+    return {"workload": wl.name, "samples_per_frame": n, "gsamples_per_s": n / ms / 1e6,
+            "fps": 1e3 / ms, "ms_per_frame": ms, "cpu_port_gsamples_per_s": cpu["value"],
+            "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
+            "error_vs_fp64_oracle": accuracy(dev, wl, [cam], p)}
 
 
 def run_reference(args):
@@ -488,8 +576,11 @@ def run_ours(args):
         cpu, _ = cpu_sample(wl, cam, params, args.cpu_seconds)
     scene.close()
     others = {}
+    main_acc = None
     if world == 1 and not args.no_configs:
         torch.cuda.synchronize()
+        main_acc = accuracy(dev, wl, [cam], params)
+        others["plain_64"] = bench_plain_small(dev)
         others["hex"] = bench_hex(dev)
         others["batched"] = bench_batch(dev)
         others["differentiable"] = bench_diff(dev)
@@ -515,6 +606,7 @@ def run_ours(args):
                      "avg_launch_ms": avg_launch_s * 1e3,
                      "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": cpu,
+        "error_vs_fp64_oracle": main_acc,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": field_bytes,
                 "d2h_bytes_per_step": pixels * BYTES_PER_PIXEL,
