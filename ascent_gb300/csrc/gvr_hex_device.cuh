@@ -23,8 +23,12 @@
 namespace gvr {
 
 constexpr int kHexNewtonSteps = 10;        // NewtonSolve default_max_steps
-constexpr float kHexNewtonTol = 1e-5f;     // |step|_inf in reference space
-constexpr float kHexInsideTol = 1e-4f;     // r, s, t in [-tol, 1 + tol]
+// FP32 positions resolve a cell of a 200^3 unit-cube mesh to ~1e-5 in
+// reference units, so steps are accepted below 1e-4 (a few ulps of the
+// physical position) and the inside test allows 2e-4: tighter bounds leave
+// samples near faces unlocated in every neighbouring cell.
+constexpr float kHexNewtonTol = 1e-4f;     // |step|_inf in reference space
+constexpr float kHexInsideTol = 2e-4f;     // r, s, t in [-tol, 1 + tol]
 constexpr int kHexStack = 64;
 
 __device__ __forceinline__ void hex_load(const DomainDev &dm, int cell, float4 (&v)[8])

@@ -672,7 +672,7 @@ static int hex_newton(const or_domain *d, int64_t c, const REAL p[3], REAL rst[3
     X[i][0] = d->hx[nid]; X[i][1] = d->hy[nid]; X[i][2] = d->hz[nid];
   }
   const REAL tol = sizeof(REAL) == 8 ? (REAL)1e-10 : (REAL)1e-5;
-  const REAL in_tol = (REAL)1e-4;
+  const REAL in_tol = (REAL)2e-4; /* the device's inside tolerance */
   REAL r = rst[0], sv = rst[1], t = rst[2];
   int conv = 0;
   for (int it = 0; it < 10; ++it) {
