@@ -330,6 +330,38 @@ GVR_API int gvr_diff_render_backward(const float *field, const int dims[3],
                                      const float *grad_rgba, const float *workspace,
                                      float *grad_field, float *grad_lut, void *stream);
 
+/* One ray segment's composited colour: the record of VolumePartial<float>
+ * (vtkh/compositing/VolumePartial.hpp:13-20), 24 bytes. rgb is
+ * premultiplied by alpha; depth orders the partials of one pixel. */
+typedef struct {
+  int32_t pixel_id;
+  float depth;
+  float rgb[3];
+  float alpha;
+} gvr_partial;
+
+/* Composite partials into one record per pixel. Replaces
+ * PartialCompositor<VolumePartial<float>>::composite
+ * (vtkh/compositing/PartialCompositor.cpp:494-547: merge :244-325, then
+ * composite_partials :331-490 and BlendPartials :57-90) for the partials of
+ * all images laid end to end in `partials` (n records).
+ *
+ * Records are ordered by (pixel_id, depth) — records with equal keys keep
+ * their input order — and each pixel's records are blended front to back
+ * with VolumePartial::blend (VolumePartial.hpp:53-62), keeping the front
+ * record's depth. Output order is the reference's: pixels with a single
+ * record first, then blended pixels, each group in pixel order. `out`
+ * needs room for n records and must not overlap `partials`; *n_out
+ * receives the count. Blend arithmetic is
+ * FP32 with no fused multiply-add, so results equal the reference compiled
+ * without contraction bit for bit.
+ *
+ * location says where both `partials` and `out` live (GVR_MEM_HOST or
+ * GVR_MEM_DEVICE). Scratch is allocated per call (about 40 bytes per
+ * record); the call returns after the result is complete. */
+GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_partial *out,
+                                   int64_t *n_out, int location, void *stream);
+
 /* Render one uniform domain without allocating any device memory; no
  * counterpart in the reference. For callers that may not call cudaMalloc or
  * cudaFree — typically a simulation that gives all GPU memory to its own

@@ -193,5 +193,45 @@ def composite_partials(images, precision: int = 64, reference: bool = False) -> 
     return out[:n].copy()
 
 
+def composite_partials_f32(images) -> np.ndarray:
+    """FP32 restatement of PartialCompositor::composite in the reference's
+    output order (vtkh/compositing/PartialCompositor.cpp:331-490): records
+    sorted by (pixel_id, depth) with the input position as the final key;
+    single-record pixels first, then blended pixels, each in pixel order;
+    blend of VolumePartial::blend (VolumePartial.hpp:53-62) as separately
+    rounded float32 operations (numpy never fuses a multiply-add).
+
+    Vectorised over pixels: pass k blends every pixel's k-th record."""
+    flat = (np.concatenate([np.asarray(im, PARTIAL_DTYPE) for im in images]) if len(images)
+            else np.zeros(0, PARTIAL_DTYPE))
+    n = len(flat)
+    if n == 0:
+        return np.zeros(0, PARTIAL_DTYPE)
+    order = np.lexsort((np.arange(n), flat["depth"], flat["pixel_id"]))
+    s = flat[order]
+    pid = s["pixel_id"]
+    head = np.ones(n, bool)
+    head[1:] = pid[1:] != pid[:-1]
+    starts = np.nonzero(head)[0]
+    counts = np.diff(np.append(starts, n))
+    seg = np.cumsum(head) - 1
+    rank = np.arange(n) - starts[seg]
+    res = s[starts].copy()
+    rgb, a = res["rgb"].copy(), res["alpha"].copy()
+    one = np.float32(1.0)
+    for k in range(1, int(counts.max())):
+        m = rank == k
+        g = seg[m]
+        o = s[m]
+        live = (a[g] < one) & (o["alpha"] != np.float32(0.0))
+        g, o = g[live], o[live]
+        op = (one - a[g]).astype(np.float32)
+        rgb[g] = (rgb[g] + (op[:, None] * o["rgb"]).astype(np.float32)).astype(np.float32)
+        na = (a[g] + (op * o["alpha"]).astype(np.float32)).astype(np.float32)
+        a[g] = np.minimum(na, one)
+    res["rgb"], res["alpha"] = rgb, a
+    return np.concatenate([res[counts == 1], res[counts > 1]])
+
+
 def num_threads(precision: int = 32) -> int:
     return int(load(precision).or_num_threads())

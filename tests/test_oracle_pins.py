@@ -114,3 +114,35 @@ def test_oracle_compositor_edge_cases():
     a["rgb"] = [[1, 0, 0], [0, 0.5, 0]]
     out = O.composite_partials([a])
     assert len(out) == 1 and tuple(out["rgb"][0]) == (1.0, 0.0, 0.0) and out["depth"][0] == 1.0
+
+
+def test_f32_compositor_reproduces_reference_golden_image():
+    golden = np.load(GOLDEN / "apcomp_volume_partial.npz")["rgba"]
+    images, w, h = apcomp_case()
+    assert np.array_equal(partials_to_png_rgba(O.composite_partials_f32(images), w, h), golden)
+
+
+@pytest.mark.skipif(O.load_apcomp_reference() is None, reason="reference apcomp not built here")
+@pytest.mark.parametrize("seed,n_images,ties", [(0, 2, False), (1, 4, False), (2, 8, False),
+                                                (3, 3, True), (4, 1, False), (5, 16, False)])
+def test_f32_compositor_equals_reference_apcomp_bytewise(seed, n_images, ties):
+    """The FP32 restatement that pins the device compositor writes the
+    reference's records, in the reference's order, byte for byte."""
+    rng = np.random.default_rng(seed)
+    ims = _random_partials(rng, n_images, ties=ties)
+    ref = O.composite_partials(ims, reference=True)
+    got = O.composite_partials_f32(ims)
+    assert ref.tobytes() == got.tobytes()
+
+
+def test_f32_compositor_edge_cases():
+    assert len(O.composite_partials_f32([])) == 0
+    a = np.zeros(3, O.PARTIAL_DTYPE)
+    a["pixel_id"] = [9, 9, 4]
+    a["depth"] = [2.0, 1.0, 0.5]
+    a["alpha"] = [0.5, 1.0, 0.25]
+    a["rgb"] = [[0, 0.5, 0], [1, 0, 0], [0, 0, 0.25]]
+    out = O.composite_partials_f32([a])
+    # pixel 4 (one record) first, then pixel 9, whose opaque front record wins
+    assert list(out["pixel_id"]) == [4, 9]
+    assert tuple(out["rgb"][1]) == (1.0, 0.0, 0.0) and out["depth"][1] == 1.0
