@@ -20,12 +20,14 @@
 //   dL/dc_k = T_k a_k g_rgb,
 //   dL/da_k = T_k (g_rgb . (c_k - R'_k) + g_A (1 - A'_k)),
 //   R'_{k-1} = a_k c_k + (1 - a_k) R'_k,  A'_{k-1} = a_k + (1 - a_k) A'_k.
-// LUT gradients accumulate in up to 16 private shared-memory copies per CTA
-// (lane l uses copy l % 16, so neighbouring rays that hit the same entry do
-// not serialise on one address), summed once per CTA; field gradients are
+// LUT gradients are summed in registers while consecutive samples of a ray
+// stay in one LUT interval, then added to one of up to 16 private
+// shared-memory copies per CTA (lane l uses copy l % 16, so neighbouring
+// rays that hit the same entry do not serialise on one address), summed once
+// per CTA; field gradients are
 // summed per ray while consecutive samples stay in one cell, then combined
-// across the lanes of a warp that hit the same cell (__match_any_sync) and
-// added to the eight corners with one atomic per distinct node.
+// with the neighbouring lane's sums when both leave the same cell at the
+// same step, and added to the eight corners with one atomic per node.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -37,6 +39,7 @@ namespace gvr {
 namespace {
 
 constexpr int kDiffK = 64;          // samples per transmittance checkpoint
+constexpr int kSub = 8;             // backward: scalars loaded together
 constexpr int kMaxDiffViews = 64;
 constexpr int kDiffLut = 4096;
 
@@ -125,6 +128,15 @@ __device__ __forceinline__ float diff_value(const float *__restrict__ f, const D
   return lerp2(lerp2(c00, c10, w[1]), lerp2(c01, c11, w[1]), w[2]);
 }
 
+// Opacity of the linear LUT lookup at scalar v (the w of diff_lut), from the
+// LUT's opacity column.
+__device__ __forceinline__ float lut_alpha(const float *lut_a, const DiffParams &p, float v)
+{
+  const float x = __saturatef((v - p.scalar_min) * p.inv_range) * (float)(p.lut_size - 1);
+  const int i0 = min((int)x, p.lut_size - 2);
+  return lerp2(lut_a[i0], lut_a[i0 + 1], x - (float)i0);
+}
+
 // Linear LUT lookup at scalar v; also returns the entry index i0 and weight.
 __device__ __forceinline__ float4 diff_lut(const float4 *lut, const DiffParams &p, float v,
                                            float &s_raw, int &i0, float &wl)
@@ -185,36 +197,45 @@ diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews 
   rgba[ray] = acc;
 }
 
-// Add g8 (the gradients of one cell's eight corners) to the field gradient,
-// after summing it over the lanes of the warp that carry the same cell.
+// Add g8 (the gradients of one cell's eight corners) to the field gradient.
+// Warp-aggregated in pairs: lanes 2i and 2i + 1 (neighbouring pixels in x)
+// that flush the same cell at the same step add their sums first, so one
+// atomic per corner covers both. Measured against pooling whole peer sets
+// (__match_any_sync, then shuffles) and against 2x2 / 4x2 pixel groups,
+// pairs were fastest: wider groups cost more shuffles than they save
+// atomics. Called by all lanes of the warp.
 __device__ __forceinline__ void flush_cell(float *__restrict__ gfield, const DiffGrid &g,
                                            int64_t base, const float g8[8], bool active)
 {
-  const unsigned act = __ballot_sync(0xffffffffu, active);
-  if (!active) return;
-  const unsigned peers = __match_any_sync(act, (unsigned long long)base);
   const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
+  const int64_t ob = __shfl_xor_sync(0xffffffffu, active ? base : -1 - (int64_t)lane, 1);
+  const bool pair = active && ob == base;
   float s[8];
 #pragma unroll
-  for (int m = 0; m < 8; ++m) s[m] = g8[m];
-  // sum over the other peers (their values fetched one by one)
-  unsigned rest = peers & ~(1u << leader);
-  while (rest) {
-    const int src = __ffs(rest) - 1;
-    rest &= rest - 1;
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const float x = __shfl_sync(peers, g8[m], src);
-      if (lane == leader) s[m] += x;
-    }
+  for (int m = 0; m < 8; ++m) {
+    const float x = __shfl_xor_sync(0xffffffffu, g8[m], 1);
+    s[m] = g8[m] + (pair ? x : 0.f);
   }
-  if (lane != leader) return;
+  if (!active || (pair && (lane & 1))) return;
   const int64_t sy = g.dims[0], sz = (int64_t)g.dims[0] * g.dims[1];
   const int64_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
 #pragma unroll
   for (int m = 0; m < 8; ++m)
     if (s[m] != 0.f) atomicAdd(gfield + base + off[m], s[m]);
+}
+
+// Add the register sums of LUT interval li (entries li and li + 1) to a
+// shared-memory copy of the LUT gradient (floats `stride` apart) and clear
+// them.
+__device__ __forceinline__ void flush_lut(float *copy, int stride, int li, float (&lg)[8])
+{
+  if (li < 0) return;
+  float *q = copy + 4 * li * stride;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    if (lg[m] != 0.f) atomicAdd(q + m * stride, lg[m]);
+    lg[m] = 0.f;
+  }
 }
 
 __global__ void __launch_bounds__(256)
@@ -225,18 +246,22 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
 {
   extern __shared__ float4 smem[];
   float4 *lut = smem;
-  // LUT gradient: p.lut_copies private copies of 4 * lut_size floats, one
-  // float of padding apart so that equal entries of different copies sit in
-  // different banks; lane l adds into copy l % lut_copies, so the lanes of a
-  // warp that hit the same entry mostly hit different addresses
+  // LUT gradient: p.lut_copies (a power of two <= 16) private copies of
+  // 4 * lut_size floats, one float of padding apart so that equal entries of
+  // different copies sit in different banks; lane l adds into copy
+  // l % copies, so the lanes of a warp that hit the same entry mostly hit
+  // different addresses. (Interleaving the copies float by float bounds bank
+  // conflicts at two lanes but measured slower: lanes l and l + 16 then
+  // collide on one address whenever they hit the same entry.)
   float *lut_a = reinterpret_cast<float *>(smem + p.lut_size);  // opacity column
   float *slg = lut_a + p.lut_size;
+  const int nc = p.lut_copies;
   const int cstride = 4 * p.lut_size + 1;
   for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) {
     lut[i] = g_lut[i];
     lut_a[i] = g_lut[i].w;
   }
-  for (int i = threadIdx.x; i < cstride * p.lut_copies; i += blockDim.x) slg[i] = 0.f;
+  for (int i = threadIdx.x; i < cstride * nc; i += blockDim.x) slg[i] = 0.f;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -265,93 +290,111 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
   int max_seg = nseg;
   for (int off = 16; off > 0; off >>= 1) max_seg = max(max_seg, __shfl_xor_sync(0xffffffffu, max_seg, off));
   float Rr = 0.f, Rg = 0.f, Rb = 0.f, Ra = 0.f;  // suffix composite behind the sample
-  float T[kDiffK];
   int64_t cur = -1;
   float g8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  int li = -1;  // LUT interval of the register sums lg
+  float lg[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const int64_t vcache = p.v_offset + ray;
+  float T[kDiffK];
   for (int sidx = max_seg - 1; sidx >= 0; --sidx) {
-    const bool seg_on = sidx < nseg;
-    const int k0 = sidx * kDiffK, k1 = min(k0 + kDiffK, n);
+    const int k0 = sidx * kDiffK, k1 = sidx < nseg ? min(k0 + kDiffK, n) : k0;
     // transmittance of every sample of the segment, forward from its
-    // checkpoint through the cached scalars (no field loads)
-    if (seg_on) {
+    // checkpoint through the cached scalars (no field loads); the scalars
+    // are loaded kSub at a time so that their latencies overlap
+    if (k1 > k0) {
       float Tr = ws[ray * p.n_seg + sidx];
-      const float nm1 = (float)(p.lut_size - 1);
-      for (int k = k0; k < k1; ++k) {
-        const float val = ws[p.v_offset + (int64_t)k * p.n_rays + ray];
-        const float x = __saturatef((val - p.scalar_min) * p.inv_range) * nm1;
-        const int i0 = min((int)x, p.lut_size - 2);
-        const float a = lerp2(lut_a[i0], lut_a[i0 + 1], x - (float)i0);
-        T[k - k0] = Tr;
-        Tr *= 1.f - a;
-      }
-    }
-    // walk it back to front (uniform trip count across the warp)
-    for (int j = kDiffK - 1; j >= 0; --j) {
-      const int k = k0 + j;
-      const bool on = seg_on && k < k1;
-      int64_t base = -1;
-      float w[3] = {0.f, 0.f, 0.f}, dv = 0.f;
-      if (on) {
-        const float t = fmaf((float)k, p.sample_dist, t0);
-        base = diff_cell(g, A, B, t, w);
-        float s_raw, wl;
-        int i0;
-        const float4 c = diff_lut(lut, p, ws[p.v_offset + (int64_t)k * p.n_rays + ray], s_raw, i0, wl);
-        const float Tk = T[j];
-        const float ta = Tk * c.w;
-        const float dcr = ta * gr.x, dcg = ta * gr.y, dcb = ta * gr.z;
-        const float da = Tk * (gr.x * (c.x - Rr) + gr.y * (c.y - Rg) + gr.z * (c.z - Rb) +
-                               gr.w * (1.f - Ra));
-        Rr = fmaf(c.w, c.x, (1.f - c.w) * Rr);
-        Rg = fmaf(c.w, c.y, (1.f - c.w) * Rg);
-        Rb = fmaf(c.w, c.z, (1.f - c.w) * Rb);
-        Ra = c.w + (1.f - c.w) * Ra;
-        // transfer-function entries i0 and i0 + 1
-        const float w0 = 1.f - wl;
-        float *q = slg + (lane % p.lut_copies) * cstride + 4 * i0;
-        atomicAdd(q + 0, w0 * dcr);
-        atomicAdd(q + 1, w0 * dcg);
-        atomicAdd(q + 2, w0 * dcb);
-        atomicAdd(q + 3, w0 * da);
-        atomicAdd(q + 4, wl * dcr);
-        atomicAdd(q + 5, wl * dcg);
-        atomicAdd(q + 6, wl * dcb);
-        atomicAdd(q + 7, wl * da);
-        // scalar: d(rgba)/dx = lut[i0 + 1] - lut[i0], x = s (n - 1)
-        if (s_raw > 0.f && s_raw < 1.f) {
-          const float4 a0 = lut[i0], a1 = lut[i0 + 1];
-          const float dx = dcr * (a1.x - a0.x) + dcg * (a1.y - a0.y) + dcb * (a1.z - a0.z) +
-                           da * (a1.w - a0.w);
-          dv = dx * (float)(p.lut_size - 1) * p.inv_range;
+      for (int kq = k0; kq < k1; kq += kSub) {
+        float vv[kSub];
+#pragma unroll
+        for (int j = 0; j < kSub; ++j) vv[j] = kq + j < k1 ? ws[vcache + (int64_t)(kq + j) * p.n_rays] : 0.f;
+#pragma unroll
+        for (int j = 0; j < kSub; ++j) {
+          T[kq - k0 + j] = Tr;
+          if (kq + j < k1) Tr *= 1.f - lut_alpha(lut_a, p, vv[j]);
         }
       }
-      // pool the field gradient per cell; flush when a lane changes cell
-      const bool change = on && base != cur && cur >= 0;
-      if (__any_sync(0xffffffffu, change)) flush_cell(gfield, g, cur, g8, change);
-      if (change) {
+    }
+    // walk it back to front (uniform trip count across the warp); the
+    // scalar and transmittance of the next sample are loaded one step ahead
+    {
+      float v_next = k1 > k0 + kDiffK - 1 ? ws[vcache + (int64_t)(k0 + kDiffK - 1) * p.n_rays] : 0.f;
+      float t_next = T[kDiffK - 1];
+      for (int j = kDiffK - 1; j >= 0; --j) {
+        const int k = k0 + j;
+        const bool on = k < k1;
+        const float v_cur = v_next, Tk = t_next;
+        if (j > 0) {
+          v_next = k - 1 < k1 ? ws[vcache + (int64_t)(k - 1) * p.n_rays] : 0.f;
+          t_next = T[j - 1];
+        }
+        int64_t base = -1;
+        float w[3] = {0.f, 0.f, 0.f}, dv = 0.f;
+        if (on) {
+          const float t = fmaf((float)k, p.sample_dist, t0);
+          base = diff_cell(g, A, B, t, w);
+          float s_raw, wl;
+          int i0;
+          const float4 c = diff_lut(lut, p, v_cur, s_raw, i0, wl);
+          const float ta = Tk * c.w;
+          const float dcr = ta * gr.x, dcg = ta * gr.y, dcb = ta * gr.z;
+          const float da = Tk * (gr.x * (c.x - Rr) + gr.y * (c.y - Rg) + gr.z * (c.z - Rb) +
+                                 gr.w * (1.f - Ra));
+          Rr = fmaf(c.w, c.x, (1.f - c.w) * Rr);
+          Rg = fmaf(c.w, c.y, (1.f - c.w) * Rg);
+          Rb = fmaf(c.w, c.z, (1.f - c.w) * Rb);
+          Ra = c.w + (1.f - c.w) * Ra;
+          // transfer-function entries i0 and i0 + 1: summed in registers
+          // while consecutive samples stay in one LUT interval
+          if (i0 != li) {
+            flush_lut(slg + (lane & (nc - 1)) * cstride, 1, li, lg);
+            li = i0;
+          }
+          const float w0 = 1.f - wl;
+          lg[0] = fmaf(w0, dcr, lg[0]);
+          lg[1] = fmaf(w0, dcg, lg[1]);
+          lg[2] = fmaf(w0, dcb, lg[2]);
+          lg[3] = fmaf(w0, da, lg[3]);
+          lg[4] = fmaf(wl, dcr, lg[4]);
+          lg[5] = fmaf(wl, dcg, lg[5]);
+          lg[6] = fmaf(wl, dcb, lg[6]);
+          lg[7] = fmaf(wl, da, lg[7]);
+          // scalar: d(rgba)/dx = lut[i0 + 1] - lut[i0], x = s (n - 1)
+          if (s_raw > 0.f && s_raw < 1.f) {
+            const float4 a0 = lut[i0], a1 = lut[i0 + 1];
+            const float dx = dcr * (a1.x - a0.x) + dcg * (a1.y - a0.y) + dcb * (a1.z - a0.z) +
+                             da * (a1.w - a0.w);
+            dv = dx * (float)(p.lut_size - 1) * p.inv_range;
+          }
+        }
+        // pool the field gradient per cell; flush when a lane changes cell
+        const bool change = on && base != cur && cur >= 0;
+        flush_cell(gfield, g, cur, g8, change);
+        if (change) {
 #pragma unroll
-        for (int m = 0; m < 8; ++m) g8[m] = 0.f;
-      }
-      if (on) {
-        cur = base;
-        const float x0 = 1.f - w[0], y0 = 1.f - w[1], z0 = 1.f - w[2];
-        g8[0] = fmaf(dv, x0 * y0 * z0, g8[0]);
-        g8[1] = fmaf(dv, w[0] * y0 * z0, g8[1]);
-        g8[2] = fmaf(dv, x0 * w[1] * z0, g8[2]);
-        g8[3] = fmaf(dv, w[0] * w[1] * z0, g8[3]);
-        g8[4] = fmaf(dv, x0 * y0 * w[2], g8[4]);
-        g8[5] = fmaf(dv, w[0] * y0 * w[2], g8[5]);
-        g8[6] = fmaf(dv, x0 * w[1] * w[2], g8[6]);
-        g8[7] = fmaf(dv, w[0] * w[1] * w[2], g8[7]);
+          for (int m = 0; m < 8; ++m) g8[m] = 0.f;
+        }
+        if (on) {
+          cur = base;
+          const float x0 = 1.f - w[0], y0 = 1.f - w[1], z0 = 1.f - w[2];
+          g8[0] = fmaf(dv, x0 * y0 * z0, g8[0]);
+          g8[1] = fmaf(dv, w[0] * y0 * z0, g8[1]);
+          g8[2] = fmaf(dv, x0 * w[1] * z0, g8[2]);
+          g8[3] = fmaf(dv, w[0] * w[1] * z0, g8[3]);
+          g8[4] = fmaf(dv, x0 * y0 * w[2], g8[4]);
+          g8[5] = fmaf(dv, w[0] * y0 * w[2], g8[5]);
+          g8[6] = fmaf(dv, x0 * w[1] * w[2], g8[6]);
+          g8[7] = fmaf(dv, w[0] * w[1] * w[2], g8[7]);
+        }
       }
     }
   }
   flush_cell(gfield, g, cur, g8, cur >= 0);
+  flush_lut(slg + (lane & (nc - 1)) * cstride, 1, li, lg);
   __syncthreads();
   for (int i = threadIdx.x; i < 4 * p.lut_size; i += blockDim.x)
   {
     float acc = 0.f;
-    for (int c = 0; c < p.lut_copies; ++c) acc += slg[c * cstride + i];
+    for (int c = 0; c < nc; ++c) acc += slg[c * cstride + i];
     if (acc != 0.f) atomicAdd(glut + i, acc);
   }
 }
@@ -455,7 +498,8 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
     return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL buffer");
   // up to 16 private LUT-gradient copies within ~72 KB of shared memory
   const size_t per_copy = sizeof(float) * (4 * (size_t)p.lut_size + 1);
-  p.lut_copies = (int)std::max<size_t>(1, std::min<size_t>(16, (72u << 10) / per_copy));
+  p.lut_copies = 16;
+  while (p.lut_copies > 1 && per_copy * p.lut_copies > (72u << 10)) p.lut_copies >>= 1;
   const size_t smem = (sizeof(float4) + sizeof(float)) * p.lut_size + per_copy * p.lut_copies;
   cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
