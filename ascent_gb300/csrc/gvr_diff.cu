@@ -314,12 +314,14 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
         }
       }
     }
-    // walk it back to front (uniform trip count across the warp); the
-    // scalar and transmittance of the next sample are loaded one step ahead
+    // walk it back to front, from the warp's last sample in the segment
+    // (uniform trip count across the warp); the scalar and transmittance of
+    // the next sample are loaded one step ahead
     {
-      float v_next = k1 > k0 + kDiffK - 1 ? ws[vcache + (int64_t)(k0 + kDiffK - 1) * p.n_rays] : 0.f;
-      float t_next = T[kDiffK - 1];
-      for (int j = kDiffK - 1; j >= 0; --j) {
+      const int jn = (int)__reduce_max_sync(0xffffffffu, (unsigned)(k1 - k0));
+      float v_next = k1 > k0 + jn - 1 ? ws[vcache + (int64_t)(k0 + jn - 1) * p.n_rays] : 0.f;
+      float t_next = T[max(jn - 1, 0)];
+      for (int j = jn - 1; j >= 0; --j) {
         const int k = k0 + j;
         const bool on = k < k1;
         const float v_cur = v_next, Tk = t_next;
