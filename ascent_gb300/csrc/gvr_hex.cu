@@ -303,6 +303,79 @@ __global__ void node_range_kernel(const float4 *__restrict__ nodes, int64_t n, f
   }
 }
 
+// Faces of a VTK hexahedron as local node ids, numbered like
+// hex_exit_face: r = 0, r = 1, s = 0, s = 1, t = 0, t = 1.
+__constant__ int kHexFace[6][4] = {{0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4},
+                                   {3, 2, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+
+// The three smallest node ids of face f (= 6 * cell + local face), ascending.
+// In a conforming mesh two faces share at most an edge, so the triple names
+// the face.
+__device__ __forceinline__ void face_triple(const int4 *__restrict__ conn, uint32_t f,
+                                            uint32_t t[3])
+{
+  const int64_t cell = f / 6;
+  const int k = f % 6;
+  const int4 a = conn[2 * cell], b = conn[2 * cell + 1];
+  const int ids[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  uint32_t n0 = (uint32_t)ids[kHexFace[k][0]], n1 = (uint32_t)ids[kHexFace[k][1]];
+  uint32_t n2 = (uint32_t)ids[kHexFace[k][2]], n3 = (uint32_t)ids[kHexFace[k][3]];
+  uint32_t x;
+#define CSWAP(p, q) if (p > q) { x = p; p = q; q = x; }
+  CSWAP(n0, n1); CSWAP(n2, n3); CSWAP(n0, n2); CSWAP(n1, n3); CSWAP(n1, n2);
+#undef CSWAP
+  t[0] = n0;
+  t[1] = n1;
+  t[2] = n2;
+}
+
+// First sort key: the largest id of the triple; value: the face.
+__global__ void face_key_kernel(const int4 *__restrict__ conn, int64_t nf, uint32_t *__restrict__ key,
+                                uint32_t *__restrict__ face)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t t[3];
+    face_triple(conn, (uint32_t)i, t);
+    key[i] = t[2];
+    face[i] = (uint32_t)i;
+  }
+}
+
+// Second sort key, in the first sort's order: the two smallest ids.
+__global__ void face_key2_kernel(const int4 *__restrict__ conn, const uint32_t *__restrict__ face,
+                                 int64_t nf, uint64_t *__restrict__ key)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t t[3];
+    face_triple(conn, face[i], t);
+    key[i] = ((uint64_t)t[0] << 32) | t[1];
+  }
+}
+
+// Faces sorted by triple: equal neighbours in the order are the two sides of
+// one face.
+__global__ void face_pair_kernel(const int4 *__restrict__ conn, const uint32_t *__restrict__ face,
+                                 int64_t nf, int *__restrict__ nbr)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t t[3], u[3];
+    face_triple(conn, face[i], t);
+    int other = -1;
+    if (i + 1 < nf) {
+      face_triple(conn, face[i + 1], u);
+      if (u[0] == t[0] && u[1] == t[1] && u[2] == t[2]) other = (int)(face[i + 1] / 6);
+    }
+    if (other < 0 && i > 0) {
+      face_triple(conn, face[i - 1], u);
+      if (u[0] == t[0] && u[1] == t[1] && u[2] == t[2]) other = (int)(face[i - 1] / 6);
+    }
+    nbr[face[i]] = other;
+  }
+}
+
 int grid_for(int64_t n, int threads = 256)
 {
   int64_t b = (n + threads - 1) / threads;
@@ -342,6 +415,8 @@ void free_hex(Domain &d)
   cudaFree(d.d_right);
   cudaFree(d.d_parent);
   cudaFree(d.d_inner_box);
+  cudaFree(d.d_nbr);
+  d.d_nbr = nullptr;
   d.d_nodes = nullptr;
   d.d_conn = nullptr;
   d.d_bvh = nullptr;
@@ -416,6 +491,58 @@ int hex_update_field(Domain &d, const void *field, int dtype, int64_t stride, in
 }
 
 // Build everything a hex domain needs on the device; fills d.dev and bounds.
+// Face-neighbour table: 6 cell ids per cell (-1 on the boundary), from two
+// stable radix sorts of the faces by their node-id triples.
+static int build_neighbours(Domain &d)
+{
+  const auto t0 = std::chrono::steady_clock::now();
+  const int64_t nf = 6 * d.n_cells;
+  uint32_t *key = nullptr, *key_tmp = nullptr, *face = nullptr, *face_tmp = nullptr, *scr = nullptr;
+  uint64_t *key2 = nullptr, *key2_tmp = nullptr;
+  int rc = GVR_OK;
+  cudaError_t e = cudaSuccess;
+  int bits = 1;
+  while (bits < 32 && ((int64_t)1 << bits) < d.n_nodes) ++bits;
+#define NB_TRY(expr, what)                                   \
+  do {                                                       \
+    e = (expr);                                              \
+    if (e != cudaSuccess) { rc = cuda_error(e, what); goto done; } \
+  } while (0)
+  NB_TRY(dev_alloc(&d.d_nbr, nf), "alloc neighbours");
+  NB_TRY(dev_alloc(&key, nf), "alloc face keys");
+  NB_TRY(dev_alloc(&key_tmp, nf), "alloc face keys");
+  NB_TRY(dev_alloc(&face, nf), "alloc faces");
+  NB_TRY(dev_alloc(&face_tmp, nf), "alloc faces");
+  NB_TRY(dev_alloc(&scr, sort_scratch_words(nf)), "alloc sort");
+  face_key_kernel<<<grid_for(nf), 256>>>(d.d_conn, nf, key, face);
+  count_launch();
+  NB_TRY(radix_sort_pairs<uint32_t>(key, face, key_tmp, face_tmp, nf, bits, scr, 0), "sort faces");
+  cudaFree(key);
+  cudaFree(key_tmp);
+  key = key_tmp = nullptr;
+  NB_TRY(dev_alloc(&key2, nf), "alloc face keys");
+  NB_TRY(dev_alloc(&key2_tmp, nf), "alloc face keys");
+  face_key2_kernel<<<grid_for(nf), 256>>>(d.d_conn, face, nf, key2);
+  count_launch();
+  NB_TRY(radix_sort_pairs<uint64_t>(key2, face, key2_tmp, face_tmp, nf, 32 + bits, scr, 0),
+         "sort faces");
+  face_pair_kernel<<<grid_for(nf), 256>>>(d.d_conn, face, nf, d.d_nbr);
+  count_launch();
+  NB_TRY(cudaGetLastError(), "neighbour launch");
+  NB_TRY(cudaDeviceSynchronize(), "neighbours");
+done:
+#undef NB_TRY
+  cudaFree(key);
+  cudaFree(key_tmp);
+  cudaFree(key2);
+  cudaFree(key2_tmp);
+  cudaFree(face);
+  cudaFree(face_tmp);
+  cudaFree(scr);
+  d.nbr_build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
 static int build_hex(Domain &d, const void *x, const void *y, const void *z, int cdtype,
                      const void *conn, int idtype, const void *field, int fdtype, int assoc,
                      int location)
@@ -540,6 +667,8 @@ done:
   cudaFree(sort_scr);
   cudaFree(counters);
   d.bvh_build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (rc == GVR_OK) rc = build_neighbours(d);
+  d.dev.hex_nbr = d.d_nbr;
   d.dev.hex_nodes = d.d_nodes;
   d.dev.hex_conn = d.d_conn;
   d.dev.hex_bvh = d.d_bvh;
@@ -563,8 +692,8 @@ int gvr_scene_add_hex(gvr_scene *s, int64_t n_nodes, const void *x, const void *
     return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
   if (n_nodes < 8 || n_cells < 1)
     return set_error(GVR_ERR_INVALID_ARGUMENT, "a hex domain needs >= 8 nodes and >= 1 cell");
-  if (n_nodes >= ((int64_t)1 << 31) || n_cells >= ((int64_t)1 << 30))
-    return set_error(GVR_ERR_UNSUPPORTED, "hex domains hold < 2^31 nodes and < 2^30 cells");
+  if (n_nodes >= ((int64_t)1 << 31) || n_cells >= ((int64_t)1 << 29))
+    return set_error(GVR_ERR_UNSUPPORTED, "hex domains hold < 2^31 nodes and < 2^29 cells");
   if ((coord_dtype != GVR_DTYPE_FLOAT32 && coord_dtype != GVR_DTYPE_FLOAT64) ||
       (dtype != GVR_DTYPE_FLOAT32 && dtype != GVR_DTYPE_FLOAT64))
     return set_error(GVR_ERR_UNSUPPORTED, "coordinates and field must be float32 or float64");
@@ -629,6 +758,19 @@ int gvr_scene_hex_bvh(const gvr_scene *s, int domain_id, uint32_t *codes, uint32
   }
   if (e != cudaSuccess) return cuda_error(e, "copy BVH");
   if (build_ms) *build_ms = d.bvh_build_ms;
+  return GVR_OK;
+}
+
+int gvr_scene_hex_neighbors(const gvr_scene *s, int domain_id, int32_t *nbr, float *build_ms)
+{
+  if (!s || domain_id < 0 || domain_id >= (int)s->domains.size())
+    return set_error(GVR_ERR_NOT_FOUND, "no such domain");
+  const Domain &d = s->domains[domain_id];
+  if (d.dev.kind != GVR_DOMAIN_HEX) return set_error(GVR_ERR_INVALID_ARGUMENT, "not a hex domain");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e == cudaSuccess && nbr) e = cudaMemcpy(nbr, d.d_nbr, sizeof(int) * 6 * d.n_cells, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "copy neighbours");
+  if (build_ms) *build_ms = d.nbr_build_ms;
   return GVR_OK;
 }
 

@@ -30,6 +30,7 @@ constexpr int kHexNewtonSteps = 10;        // NewtonSolve default_max_steps
 constexpr float kHexNewtonTol = 1e-4f;     // |step|_inf in reference space
 constexpr float kHexInsideTol = 2e-4f;     // r, s, t in [-tol, 1 + tol]
 constexpr int kHexStack = 64;
+constexpr int kHexHops = 4;                // face-neighbour steps before the LBVH walk
 
 __device__ __forceinline__ void hex_load(const DomainDev &dm, int cell, float4 (&v)[8])
 {
@@ -59,9 +60,11 @@ __device__ __forceinline__ void hex_weights(float r, float s, float t, float (&n
   n[7] = r0 * s * t;
 }
 
-// Newton's method on x(r,s,t) - p = 0 from the guess in rst; true when it
-// converged inside the element (rst then holds the reference coordinates).
-__device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3], float rst[3])
+// Newton's method on x(r,s,t) - p = 0 from the guess in rst: 1 when it
+// converged inside the element, 0 when it converged outside (rst then holds
+// the reference coordinates of p, outside [0,1]^3), -1 when it failed.
+__device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const float p[3],
+                                                 float rst[3])
 {
   float r = rst[0], s = rst[1], t = rst[2];
   bool conv = false;
@@ -91,7 +94,7 @@ __device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3
     const float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
     const float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
     const float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-    if (!(fabsf(det) > 0.f)) return false;
+    if (!(fabsf(det) > 0.f)) return -1;
     const float id = 1.f / det;
     const float c10 = J[0][2] * J[2][1] - J[0][1] * J[2][2];
     const float c11 = J[0][0] * J[2][2] - J[0][2] * J[2][0];
@@ -105,7 +108,7 @@ __device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3
     r -= d0;
     s -= d1;
     t -= d2;
-    if (!(fabsf(r) < 1e3f && fabsf(s) < 1e3f && fabsf(t) < 1e3f)) return false;
+    if (!(fabsf(r) < 1e3f && fabsf(s) < 1e3f && fabsf(t) < 1e3f)) return -1;
     if (fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2))) < kHexNewtonTol) {
       conv = true;
       break;
@@ -114,8 +117,28 @@ __device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3
   rst[0] = r;
   rst[1] = s;
   rst[2] = t;
-  return conv && r >= -kHexInsideTol && r <= 1.f + kHexInsideTol && s >= -kHexInsideTol &&
+  if (!conv) return -1;
+  return r >= -kHexInsideTol && r <= 1.f + kHexInsideTol && s >= -kHexInsideTol &&
          s <= 1.f + kHexInsideTol && t >= -kHexInsideTol && t <= 1.f + kHexInsideTol;
+}
+
+__device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3], float rst[3])
+{
+  return hex_newton_status(v, p, rst) == 1;
+}
+
+// Face through which reference coordinates rst (outside the element) leave
+// it: the most violated bound, numbered r=0, r=1, s=0, s=1, t=0, t=1.
+__device__ __forceinline__ int hex_exit_face(const float rst[3])
+{
+  int face = 0;
+  float worst = -rst[0];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (-rst[a] > worst) { worst = -rst[a]; face = 2 * a; }
+    if (rst[a] - 1.f > worst) { worst = rst[a] - 1.f; face = 2 * a + 1; }
+  }
+  return face;
 }
 
 __device__ __forceinline__ bool in_box(const float p[3], float lx, float ly, float lz, float hx,

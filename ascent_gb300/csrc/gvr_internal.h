@@ -45,6 +45,7 @@ struct DomainDev {
   const int4 *hex_conn;       // 8 node ids per cell (VTK hex order), 2 int4
   const float4 *hex_bvh;      // 4 float4 per inner node (see gvr_hex.cu)
   const int *hex_ids;         // cell id of each sorted leaf
+  const int *hex_nbr;         // 6 face neighbours per cell (r=0,r=1,s=0,s=1,t=0,t=1), -1 none
   int n_cells;
   int pad_;
 };
@@ -123,7 +124,9 @@ struct Domain {
   int32_t *d_right = nullptr;
   int32_t *d_parent = nullptr;      // 2 n_cells - 1 entries, root's is -1
   float4 *d_inner_box = nullptr;    // 2 per inner node: lo, hi
+  int *d_nbr = nullptr;             // 6 face neighbours per cell
   float bvh_build_ms = 0.f;
+  float nbr_build_ms = 0.f;
 };
 
 }  // namespace gvr

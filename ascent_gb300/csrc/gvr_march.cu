@@ -275,9 +275,11 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
 }
 
 // Hexahedral domain: each sample is located by Newton's method in the cell
-// of the previous sample (starting from its reference coordinates), and
-// only when that fails by a walk of the LBVH; the eight corner records of
-// the current cell stay in registers between samples. Samples outside every
+// of the previous sample (starting from its reference coordinates); when the
+// solution lies outside that cell, the march steps to the face neighbour it
+// left through (up to kHexHops cells), and only when that fails walks the
+// LBVH. The eight corner records of the current cell stay in registers
+// between samples. Samples outside every
 // cell contribute nothing but are counted, like the structured stepping rule.
 __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
                          const MarchParams &mp, const float4 *lut, float thr, float4 &acc)
@@ -294,7 +296,23 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
     bool found = false;
     if (cur >= 0) {
       float g[3] = {rst[0], rst[1], rst[2]};
-      if (hex_newton(v, p, g)) {
+      int st = hex_newton_status(v, p, g);
+      // left the cell: step to the neighbour across the face it left
+      // through (Newton's outside solution names it), a few times at most
+      for (int hop = 0; st == 0 && hop < kHexHops && dm.hex_nbr; ++hop) {
+        const int face = hex_exit_face(g);
+        const int nb = __ldg(dm.hex_nbr + 6 * (int64_t)cur + face);
+        if (nb < 0) break;
+        cur = nb;
+        hex_load(dm, cur, v);
+        // guess: the point's coordinates across a like-oriented face
+        g[face >> 1] += (face & 1) ? -1.f : 1.f;
+        g[0] = __saturatef(g[0]);
+        g[1] = __saturatef(g[1]);
+        g[2] = __saturatef(g[2]);
+        st = hex_newton_status(v, p, g);
+      }
+      if (st == 1) {
         found = true;
         rst[0] = g[0]; rst[1] = g[1]; rst[2] = g[2];
       }

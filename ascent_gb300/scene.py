@@ -115,6 +115,15 @@ class Scene:
                C.byref(ms))
         return ms.value
 
+    def hex_neighbors(self, domain_id: int, table: bool = True):
+        """The domain's face-neighbour table, (n_cells, 6) int32 (None when
+        table is False), and its build time in ms."""
+        nbr = np.zeros((self.hex_cells(domain_id), 6), np.int32) if table else None
+        ms = C.c_float(0)
+        N.call("gvr_scene_hex_neighbors", self.handle, int(domain_id),
+               C.c_void_p(nbr.ctypes.data) if table else None, C.byref(ms))
+        return nbr, ms.value
+
     def hex_cells(self, domain_id: int) -> int:
         return int(self._hex_cells[domain_id])
 

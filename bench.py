@@ -58,7 +58,7 @@ def parse_args():
                     help="target CPU time of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
-                    help="skip the hexahedral and batched-view configurations")
+                    help="skip the plain-64, hex, batched, differentiable and compositing configurations")
     return ap.parse_args()
 
 
@@ -217,6 +217,7 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
     V.load_workload(sc, wl)
     load_s = time.time() - t0
     build_ms = sc.hex_build_ms(0)
+    _, nbr_ms = sc.hex_neighbors(0, table=False)
     stream = torch.cuda.current_stream(dev)
     rgba = torch.empty((size, size, 4), dtype=torch.float32, device=f"cuda:{dev}")
     depth = torch.empty((size, size), dtype=torch.float32, device=f"cuda:{dev}")
@@ -233,7 +234,7 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
     return {"workload": wl.name, "cells": n_cells ** 3, "samples_per_frame": n,
             "error_vs_fp64_oracle": acc,
             "gsamples_per_s": n / ms / 1e6, "fps": 1e3 / ms, "ms_per_frame": ms,
-            "bvh_build_ms": build_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
+            "bvh_build_ms": build_ms, "face_neighbour_build_ms": nbr_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
             "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": pk["hbm_gbs"],
                          "unit": "GB/s", "frac": alg / ms / 1e6 / pk["hbm_gbs"],
                          "bytes_per_sample": 160}}
@@ -391,6 +392,48 @@ def accuracy(dev, wl, cams, params, rows=None, precision=64) -> dict:
     worst["views"] = len(cams)
     worst["oracle"] = "FP64 CPU oracle (oracle/gvr_oracle.c)"
     return worst
+
+
+def bench_composite(dev, n_images=8, size=1024, cover=0.8, reps=10) -> dict:
+    """Standalone partial compositing (PartialCompositor::composite): n_images
+    partial images of size^2 pixels, each covering a seeded `cover` fraction
+    of the pixels with random depths and premultiplied colours (seed 6);
+    records resident on the device. Checked byte for byte against the FP32
+    restatement of the reference compositor."""
+    import torch
+    from ascent_gb300 import compositing as CP
+    from oracle import oracle as O
+    rng = np.random.default_rng(6)
+    ims = []
+    for _ in range(n_images):
+        ids = np.nonzero(rng.uniform(size=size * size) < cover)[0]
+        p = np.zeros(len(ids), CP.PARTIAL_DTYPE)
+        p["pixel_id"] = ids
+        p["depth"] = rng.uniform(0, 10, len(ids)).astype(np.float32)
+        a = rng.uniform(0.001, 1.0, len(ids)).astype(np.float32)
+        p["alpha"] = a
+        p["rgb"] = (rng.uniform(0, 1, (len(ids), 3)) * a[:, None]).astype(np.float32)
+        ims.append(p)
+    flat = np.concatenate(ims)
+    d = CP.to_device(flat, f"cuda:{dev}")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        out = CP.composite_partials_device(d)
+    ms = _timed(lambda: CP.composite_partials_device(d), stream, reps)
+    out = CP.from_device(CP.composite_partials_device(d))
+    exact = out.tobytes() == O.composite_partials_f32(ims).tobytes()
+    t0 = time.perf_counter()
+    O.composite_partials(ims, precision=32)
+    cpu_s = time.perf_counter() - t0
+    alg = 24 * (len(flat) + len(out))
+    pk = peaks()
+    return {"workload": f"composite{n_images}x{size}^2@{cover}", "records": len(flat),
+            "pixels_out": len(out), "ms": ms, "grecords_per_s": len(flat) / ms / 1e6,
+            "bit_identical_to_reference_order_f32": exact,
+            "cpu_oracle_ms": cpu_s * 1e3, "cpu_oracle_kind": "oracle C compositor (qsort, 1 thread)",
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": pk["hbm_gbs"],
+                         "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / pk["hbm_gbs"],
+                         "bytes_per_record": "24 read + 24 per output record"}}
 
 
 def bench_plain_small(dev, reps=20) -> dict:
@@ -584,6 +627,7 @@ def run_ours(args):
         others["hex"] = bench_hex(dev)
         others["batched"] = bench_batch(dev)
         others["differentiable"] = bench_diff(dev)
+        others["composite"] = bench_composite(dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

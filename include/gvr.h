@@ -224,6 +224,16 @@ GVR_API int gvr_scene_hex_bvh(const gvr_scene *scene, int domain_id, uint32_t *c
                               uint32_t *ids, int32_t *left, int32_t *right,
                               int32_t *parent, float *inner_boxes, float *build_ms);
 
+/* Copy a hex domain's face-neighbour table to the host: 6 cell ids per cell
+ * (faces r=0, r=1, s=0, s=1, t=0, t=1 of the VTK hexahedron; -1 where the
+ * face is on the boundary), built on the device at ingest from a sort of the
+ * faces by their node ids. The march steps along it from cell to cell
+ * before falling back to the LBVH, as VTK-m's unstructured tracer walks
+ * cell faces (ConnectivityProxy, VolumeRenderer.cpp:182-220). build_ms (may
+ * be NULL) receives the build's wall time. */
+GVR_API int gvr_scene_hex_neighbors(const gvr_scene *scene, int domain_id, int32_t *nbr,
+                                    float *build_ms);
+
 /* Locate n points (3 n host floats) in a hex domain: cells[i] = containing
  * cell or -1, rst = reference coordinates (Devil Ray's DeviceMesh::locate,
  * data_model/device_mesh.hpp:250-360, with NewtonSolve). */

@@ -233,5 +233,34 @@ def composite_partials_f32(images) -> np.ndarray:
     return np.concatenate([res[counts == 1], res[counts > 1]])
 
 
+HEX_FACES = np.array([[0, 3, 7, 4], [1, 2, 6, 5], [0, 1, 5, 4], [3, 2, 6, 7], [0, 1, 2, 3],
+                      [4, 5, 6, 7]])
+
+
+def hex_face_neighbors(conn) -> np.ndarray:
+    """Face-neighbour table of a hex mesh, (n_cells, 6): the cell across each
+    VTK hexahedron face (r=0, r=1, s=0, s=1, t=0, t=1), -1 on the boundary.
+    Faces are identified by their three smallest node ids (two faces of a
+    conforming mesh share at most an edge) and paired by a stable sort of
+    the faces by that triple: a face takes the next face in the order when
+    it has the same triple, else the previous one."""
+    conn = np.asarray(conn, dtype=np.int64).reshape(-1, 8)
+    nc = len(conn)
+    trip = np.sort(conn[:, HEX_FACES], axis=2)[:, :, :3].reshape(-1, 3)
+    order = np.lexsort((np.arange(6 * nc), trip[:, 2], trip[:, 1], trip[:, 0]))
+    t = trip[order]
+    same_next = np.zeros(6 * nc, bool)
+    same_next[:-1] = (t[1:] == t[:-1]).all(axis=1)
+    same_prev = np.zeros(6 * nc, bool)
+    same_prev[1:] = same_next[:-1]
+    other = np.full(6 * nc, -1, np.int64)
+    idx = np.arange(6 * nc)
+    other[same_prev] = order[idx[same_prev] - 1] // 6
+    other[same_next] = order[idx[same_next] + 1] // 6
+    nbr = np.full(6 * nc, -1, np.int64)
+    nbr[order] = other
+    return nbr.reshape(nc, 6).astype(np.int32)
+
+
 def num_threads(precision: int = 32) -> int:
     return int(load(precision).or_num_threads())

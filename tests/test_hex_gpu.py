@@ -157,3 +157,45 @@ def test_hex_element_field():
     e = image_error(g, o)
     # a sample right on a face may pick either neighbour's constant value
     assert e["frac_within_2"] >= 0.99 and e["mae"] <= 2e-3, e
+
+
+def _rotated_cells(conn, seed):
+    """The same mesh with every other cell's local node order rotated a
+    quarter turn about t (still a valid VTK hexahedron), so neighbouring
+    cells disagree on orientation."""
+    rng = np.random.default_rng(seed)
+    rot = np.array([1, 2, 3, 0, 5, 6, 7, 4])
+    out = conn.copy()
+    pick = rng.uniform(size=len(conn)) < 0.5
+    out[pick] = conn[pick][:, rot]
+    return out
+
+
+@pytest.mark.parametrize("n,rotate", [(6, False), (17, False), (17, True)])
+def test_face_neighbours_bit_exact(n, rotate):
+    wl = W.hex_mesh(n_cells=n, seed=9, width=8, height=8)
+    d = wl.domains[0]
+    conn = _rotated_cells(d.conn, 2) if rotate else d.conn
+    with S.Scene(0) as sc:
+        did = sc.add_hex(d.x, d.y, d.z, conn, d.field)
+        nbr, ms = sc.hex_neighbors(did)
+    np.testing.assert_array_equal(nbr, O.hex_face_neighbors(conn))
+    assert (nbr >= 0).sum() == 6 * n ** 3 - 6 * n * n and ms >= 0
+
+
+def test_hex_render_rotated_cells_matches_oracle():
+    """Face stepping with neighbours of another orientation (the guess across
+    the face is then wrong and Newton or the LBVH must recover)."""
+    wl = W.hex_mesh(n_cells=20, seed=4, width=96, height=80)
+    d = wl.domains[0]
+    conn = _rotated_cells(d.conn, 5)
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    with S.Scene(0) as sc:
+        sc.add_hex(d.x, d.y, d.z, conn, d.field)
+        g, gd, gn = sc.render(cam, p, count_samples=True)
+    osc = O.OracleScene(64)
+    osc.add_hex(d.x, d.y, d.z, conn, d.field)
+    o, od, on = osc.render(cam, p)
+    assert o[..., 3].max() > 0.1
+    assert_parity(g, o)
