@@ -63,8 +63,12 @@ __device__ __forceinline__ void hex_weights(float r, float s, float t, float (&n
 // Newton's method on x(r,s,t) - p = 0 from the guess in rst: 1 when it
 // converged inside the element, 0 when it converged outside (rst then holds
 // the reference coordinates of p, outside [0,1]^3), -1 when it failed.
+// When it converged and `step` is given, drst receives J^-1 step with the
+// last Jacobian: the change of rst over a world-space displacement `step`
+// (the next sample's guess along a ray).
 __device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const float p[3],
-                                                 float rst[3])
+                                                 float rst[3], const float *step = nullptr,
+                                                 float *drst = nullptr)
 {
   float r = rst[0], s = rst[1], t = rst[2];
   bool conv = false;
@@ -111,6 +115,11 @@ __device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const flo
     if (!(fabsf(r) < 1e3f && fabsf(s) < 1e3f && fabsf(t) < 1e3f)) return -1;
     if (fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2))) < kHexNewtonTol) {
       conv = true;
+      if (step) {
+        drst[0] = (c00 * step[0] + c10 * step[1] + c20 * step[2]) * id;
+        drst[1] = (c01 * step[0] + c11 * step[1] + c21 * step[2]) * id;
+        drst[2] = (c02 * step[0] + c12 * step[1] + c22 * step[2]) * id;
+      }
       break;
     }
   }

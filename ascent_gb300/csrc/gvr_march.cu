@@ -275,7 +275,8 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
 }
 
 // Hexahedral domain: each sample is located by Newton's method in the cell
-// of the previous sample (starting from its reference coordinates); when the
+// of the previous sample (starting from its reference coordinates moved by
+// the last Jacobian's image of the ray step); when the
 // solution lies outside that cell, the march steps to the face neighbour it
 // left through (up to kHexHops cells), and only when that fails walks the
 // LBVH. The eight corner records of the current cell stay in registers
@@ -287,6 +288,10 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
   float4 v[8];
   int cur = -1;
   float rst[3] = {0.5f, 0.5f, 0.5f};
+  // change of rst from one sample to the next (J^-1 times the ray step,
+  // from the last Newton solve): the next sample's guess
+  float drst[3] = {0.f, 0.f, 0.f};
+  const float step[3] = {r.d[0] * mp.sample_dist, r.d[1] * mp.sample_dist, r.d[2] * mp.sample_dist};
   int count = 0;
   for (int k = 0;; ++k) {
     const float t = fmaf((float)k, mp.sample_dist, t0);
@@ -295,8 +300,8 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
     const float p[3] = {fmaf(t, r.d[0], r.o[0]), fmaf(t, r.d[1], r.o[1]), fmaf(t, r.d[2], r.o[2])};
     bool found = false;
     if (cur >= 0) {
-      float g[3] = {rst[0], rst[1], rst[2]};
-      int st = hex_newton_status(v, p, g);
+      float g[3] = {rst[0] + drst[0], rst[1] + drst[1], rst[2] + drst[2]};
+      int st = hex_newton_status(v, p, g, step, drst);
       // left the cell: step to the neighbour across the face it left
       // through (Newton's outside solution names it), a few times at most
       for (int hop = 0; st == 0 && hop < kHexHops && dm.hex_nbr; ++hop) {
@@ -310,7 +315,7 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
         g[0] = __saturatef(g[0]);
         g[1] = __saturatef(g[1]);
         g[2] = __saturatef(g[2]);
-        st = hex_newton_status(v, p, g);
+        st = hex_newton_status(v, p, g, step, drst);
       }
       if (st == 1) {
         found = true;
@@ -320,6 +325,7 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
     if (!found) {
       cur = hex_locate(dm, p, rst, v);
       found = cur >= 0;
+      drst[0] = drst[1] = drst[2] = 0.f;
     }
     if (!found) continue;
     float val;
