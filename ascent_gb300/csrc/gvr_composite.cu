@@ -2,19 +2,26 @@
 //
 // Replaces PartialCompositor<VolumePartial<float>>::composite for partials a
 // caller already holds (vtkh/compositing/PartialCompositor.cpp:244-547,
-// BlendPartials :57-90, VolumePartial::blend VolumePartial.hpp:86-95):
-//   1. sort the records by (pixel id, depth) — a stable device radix sort of
-//      64-bit keys (pixel id, order-preserving bits of the depth), so records
-//      with equal keys keep their input order;
-//   2. flag segment heads: pixels with a single record ("unique") and the
-//      first record of pixels with several;
-//   3. exclusive scans of the two flags give every output slot: unique
-//      pixels first, then blended pixels, each in pixel order — the order
-//      composite_partials writes (:422-489);
-//   4. one thread per multi-record pixel blends its records front to back
-//      with VolumePartial::blend. Its arithmetic uses explicitly rounded
-//      FP32 operations (no fused multiply-add), so the output is bit-identical
-//      to the reference compiled without FMA contraction.
+// BlendPartials :57-90, VolumePartial::blend VolumePartial.hpp:53-62). The
+// result is the reference's: records ordered by (pixel id, depth) with
+// equal keys in input order; pixels with one record are copied, the others
+// blended front to back; output = single-record pixels in pixel order, then
+// blended pixels in pixel order (composite_partials :422-489). The blend
+// uses explicitly rounded FP32 operations (no fused multiply-add), so the
+// output is bit-identical to the reference compiled without contraction.
+//
+// Two ways to group the records by pixel:
+//   dense ids (pixel range <= 2 n + 64 Ki, the normal case: ids are y*W+x)
+//     a per-pixel histogram whose atomics also hand every record its slot
+//     in its pixel's bucket, scans over the pixel range for the bucket
+//     offsets and for the output slots, and one thread per pixel that
+//     orders its few records by (depth, input index) and blends them;
+//   sparse ids
+//     a stable device radix sort of 64-bit keys (pixel id, order-preserving
+//     depth bits), segment flags and scans, one thread per blended pixel.
+// Scratch comes from the stream-ordered allocator (cudaMallocAsync), so
+// repeated calls reuse the pool.
+#include <algorithm>
 #include <cstdint>
 
 #include "gvr_internal.h"
@@ -32,6 +39,18 @@ __device__ __forceinline__ uint32_t order_bits(float f)
   uint32_t u = __float_as_uint(f);
   if (u == 0x80000000u) u = 0u;
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ void blend_into(Partial &r, const Partial &o)
+{
+  // VolumePartial::blend
+  if (r.alpha >= 1.f || o.alpha == 0.f) return;
+  const float op = __fsub_rn(1.f, r.alpha);
+  r.rgb[0] = __fadd_rn(r.rgb[0], __fmul_rn(op, o.rgb[0]));
+  r.rgb[1] = __fadd_rn(r.rgb[1], __fmul_rn(op, o.rgb[1]));
+  r.rgb[2] = __fadd_rn(r.rgb[2], __fmul_rn(op, o.rgb[2]));
+  r.alpha = __fadd_rn(r.alpha, __fmul_rn(op, o.alpha));
+  r.alpha = r.alpha > 1.f ? 1.f : r.alpha;
 }
 
 __global__ void key_kernel(const Partial *__restrict__ in, int64_t n, uint64_t *__restrict__ keys,
@@ -61,12 +80,24 @@ __global__ void flag_kernel(const uint64_t *__restrict__ keys, int64_t n, uint32
   }
 }
 
+// Unique and blended pixel counts of the sorted path: last exclusive
+// prefix plus last flag.
+__global__ void sorted_totals_kernel(const uint32_t *upos, const uint32_t *uniq, const uint32_t *mpos,
+                                     const uint32_t *multi, int64_t n, uint32_t *totals)
+{
+  if (threadIdx.x == 0) {
+    totals[0] = upos[n - 1] + uniq[n - 1];
+    totals[1] = mpos[n - 1] + multi[n - 1];
+  }
+}
+
 __global__ void emit_kernel(const Partial *__restrict__ in, const uint64_t *__restrict__ keys,
                             const uint32_t *__restrict__ idx, int64_t n,
                             const uint32_t *__restrict__ upos, const uint32_t *__restrict__ mpos,
                             const uint32_t *__restrict__ uniq, const uint32_t *__restrict__ multi,
-                            uint32_t n_unique, Partial *__restrict__ out)
+                            const uint32_t *__restrict__ totals, Partial *__restrict__ out)
 {
+  const uint32_t n_unique = totals[0];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (uniq[i]) {
@@ -74,19 +105,126 @@ __global__ void emit_kernel(const Partial *__restrict__ in, const uint64_t *__re
     } else if (multi[i]) {
       Partial r = in[idx[i]];
       const uint32_t pid = (uint32_t)(keys[i] >> 32);
-      for (int64_t j = i + 1; j < n && (uint32_t)(keys[j] >> 32) == pid; ++j) {
-        const Partial o = in[idx[j]];
-        // VolumePartial::blend
-        if (r.alpha >= 1.f || o.alpha == 0.f) continue;
-        const float op = __fsub_rn(1.f, r.alpha);
-        r.rgb[0] = __fadd_rn(r.rgb[0], __fmul_rn(op, o.rgb[0]));
-        r.rgb[1] = __fadd_rn(r.rgb[1], __fmul_rn(op, o.rgb[1]));
-        r.rgb[2] = __fadd_rn(r.rgb[2], __fmul_rn(op, o.rgb[2]));
-        r.alpha = __fadd_rn(r.alpha, __fmul_rn(op, o.alpha));
-        r.alpha = r.alpha > 1.f ? 1.f : r.alpha;
-      }
+      for (int64_t j = i + 1; j < n && (uint32_t)(keys[j] >> 32) == pid; ++j) blend_into(r, in[idx[j]]);
       out[n_unique + mpos[i]] = r;
     }
+  }
+}
+
+// Smallest and largest pixel id, as order-preserving unsigned values
+// (mm[0] starts at 0xffffffff, mm[1] at 0).
+__global__ void range_kernel(const Partial *__restrict__ in, int64_t n, unsigned *__restrict__ mm)
+{
+  unsigned lo = 0xffffffffu, hi = 0u;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned u = (unsigned)in[i].pixel_id ^ 0x80000000u;
+    lo = min(lo, u);
+    hi = max(hi, u);
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(mm, lo);
+    atomicMax(mm + 1, hi);
+  }
+}
+
+// cnt[p] = records of pixel lo + p; rank[i] = record i's slot in its bucket
+// (in arrival order; the emit kernel restores input order).
+__global__ void count_kernel(const Partial *__restrict__ in, int64_t n, int lo,
+                             uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    rank[i] = atomicAdd(cnt + (in[i].pixel_id - lo), 1u);
+}
+
+__global__ void bucket_kernel(const Partial *__restrict__ in, int64_t n, int lo,
+                              const uint32_t *__restrict__ off, const uint32_t *__restrict__ rank,
+                              uint32_t *__restrict__ order)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    order[off[in[i].pixel_id - lo] + rank[i]] = (uint32_t)i;
+}
+
+// upos[p] = 1 for pixels with one record, mpos[p] = 1 for pixels with more
+// (scanned in place afterwards into output slots).
+__global__ void pixel_flag_kernel(const uint32_t *__restrict__ cnt, int64_t r,
+                                  uint32_t *__restrict__ upos, uint32_t *__restrict__ mpos)
+{
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < r;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cnt[p];
+    upos[p] = c == 1;
+    mpos[p] = c > 1;
+  }
+}
+
+constexpr int kLocalSort = 32;  // records per pixel ordered in thread-local arrays
+
+__device__ __forceinline__ bool before(uint32_t ka, uint32_t ia, uint32_t kb, uint32_t ib)
+{
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+// One thread per pixel: copy or blend its records in (depth, input index)
+// order. totals[0..1] receive the unique and blended pixel counts.
+__global__ void pixel_emit_kernel(const Partial *__restrict__ in, const uint32_t *__restrict__ cnt,
+                                  const uint32_t *__restrict__ off, const uint32_t *__restrict__ upos,
+                                  const uint32_t *__restrict__ mpos, uint32_t *__restrict__ order,
+                                  int64_t r, Partial *__restrict__ out, uint32_t *__restrict__ totals)
+{
+  const uint32_t n_unique = upos[r - 1] + (cnt[r - 1] == 1);
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < r;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cnt[p];
+    if (p == r - 1) {
+      totals[0] = n_unique;
+      totals[1] = mpos[p] + (c > 1);
+    }
+    if (c == 0) continue;
+    uint32_t *seg = order + off[p];
+    if (c == 1) {
+      out[upos[p]] = in[seg[0]];
+      continue;
+    }
+    Partial res;
+    if (c <= kLocalSort) {
+      uint32_t key[kLocalSort], idx[kLocalSort];
+      for (uint32_t j = 0; j < c; ++j) {
+        const uint32_t i = seg[j];
+        const uint32_t k = order_bits(in[i].depth);
+        uint32_t q = j;
+        while (q > 0 && before(k, i, key[q - 1], idx[q - 1])) {
+          key[q] = key[q - 1];
+          idx[q] = idx[q - 1];
+          --q;
+        }
+        key[q] = k;
+        idx[q] = i;
+      }
+      res = in[idx[0]];
+      for (uint32_t j = 1; j < c; ++j) blend_into(res, in[idx[j]]);
+    } else {
+      // rare deep pixels: insertion sort of the bucket in place
+      for (uint32_t j = 1; j < c; ++j) {
+        const uint32_t i = seg[j];
+        const uint32_t k = order_bits(in[i].depth);
+        uint32_t q = j;
+        while (q > 0) {
+          const uint32_t pi = seg[q - 1];
+          if (!before(k, i, order_bits(in[pi].depth), pi)) break;
+          seg[q] = pi;
+          --q;
+        }
+        seg[q] = i;
+      }
+      res = in[seg[0]];
+      for (uint32_t j = 1; j < c; ++j) blend_into(res, in[seg[j]]);
+    }
+    out[n_unique + mpos[p]] = res;
   }
 }
 
@@ -94,6 +232,82 @@ int grid_of(int64_t n)
 {
   const int64_t b = (n + 255) / 256;
   return (int)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
+}
+
+// Scratch of one call, carved from a single stream-ordered allocation.
+struct Arena {
+  char *base = nullptr;
+  size_t used = 0;
+  template <typename T>
+  T *take(size_t count)
+  {
+    T *p = reinterpret_cast<T *>(base + used);
+    used += (sizeof(T) * std::max<size_t>(count, 1) + 255) & ~(size_t)255;
+    return p;
+  }
+};
+
+size_t dense_bytes(int64_t n, int64_t r)
+{
+  return 256 * 8 + (4 * (size_t)r + 2 * (size_t)n + scan_scratch_words(r) + 2) * sizeof(uint32_t);
+}
+
+size_t sorted_bytes(int64_t n)
+{
+  return 256 * 12 + (2 * sizeof(uint64_t) + 6 * sizeof(uint32_t)) * (size_t)n +
+         (sort_scratch_words(n) + scan_scratch_words(n) + 2) * sizeof(uint32_t);
+}
+
+// Dense pixel ids: histogram, bucket, per-pixel emit.
+cudaError_t composite_dense(const Partial *in, int64_t n, int lo, int64_t r, Partial *out,
+                            Arena &a, uint32_t *totals, cudaStream_t st)
+{
+  uint32_t *cnt = a.take<uint32_t>(r), *off = a.take<uint32_t>(r);
+  uint32_t *upos = a.take<uint32_t>(r), *mpos = a.take<uint32_t>(r);
+  uint32_t *rank = a.take<uint32_t>(n), *order = a.take<uint32_t>(n);
+  uint32_t *scan_tmp = a.take<uint32_t>(scan_scratch_words(r));
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * r, st);
+  if (e != cudaSuccess) return e;
+  count_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, cnt, rank);
+  count_launch();
+  if ((e = cudaMemcpyAsync(off, cnt, sizeof(uint32_t) * r, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan(off, r, scan_tmp, st)) != cudaSuccess) return e;
+  bucket_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, off, rank, order);
+  count_launch();
+  pixel_flag_kernel<<<grid_of(r), 256, 0, st>>>(cnt, r, upos, mpos);
+  count_launch();
+  if ((e = exclusive_scan(upos, r, scan_tmp, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan(mpos, r, scan_tmp, st)) != cudaSuccess) return e;
+  pixel_emit_kernel<<<grid_of(r), 256, 0, st>>>(in, cnt, off, upos, mpos, order, r, out, totals);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Any pixel ids: stable radix sort by (pixel id, depth), segment scans.
+cudaError_t composite_sorted(const Partial *in, int64_t n, Partial *out, Arena &a,
+                             uint32_t *totals, cudaStream_t st)
+{
+  uint64_t *keys = a.take<uint64_t>(n), *keys_tmp = a.take<uint64_t>(n);
+  uint32_t *idx = a.take<uint32_t>(n), *idx_tmp = a.take<uint32_t>(n);
+  uint32_t *uniq = a.take<uint32_t>(n), *multi = a.take<uint32_t>(n);
+  uint32_t *upos = a.take<uint32_t>(n), *mpos = a.take<uint32_t>(n);
+  uint32_t *scratch = a.take<uint32_t>(sort_scratch_words(n));
+  uint32_t *scan_tmp = a.take<uint32_t>(scan_scratch_words(n));
+  key_kernel<<<grid_of(n), 256, 0, st>>>(in, n, keys, idx);
+  count_launch();
+  cudaError_t e = radix_sort_pairs<uint64_t>(keys, idx, keys_tmp, idx_tmp, n, 64, scratch, st);
+  if (e != cudaSuccess) return e;
+  flag_kernel<<<grid_of(n), 256, 0, st>>>(keys, n, uniq, multi);
+  count_launch();
+  if ((e = cudaMemcpyAsync(upos, uniq, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(mpos, multi, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan(upos, n, scan_tmp, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan(mpos, n, scan_tmp, st)) != cudaSuccess) return e;
+  sorted_totals_kernel<<<1, 32, 0, st>>>(upos, uniq, mpos, multi, n, totals);
+  count_launch();
+  emit_kernel<<<grid_of(n), 256, 0, st>>>(in, keys, idx, n, upos, mpos, uniq, multi, totals, out);
+  count_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -108,85 +322,65 @@ extern "C" int gvr_composite_partials(const gvr_partial *partials, int64_t n, gv
     return set_error(GVR_ERR_INVALID_ARGUMENT, "bad partial arrays");
   if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
     return set_error(GVR_ERR_INVALID_ARGUMENT, "bad location");
-  if (n >= ((int64_t)1 << 32) - 1) return set_error(GVR_ERR_UNSUPPORTED, "at most 2^32 - 2 partials");
+  if (n >= ((int64_t)1 << 31)) return set_error(GVR_ERR_UNSUPPORTED, "at most 2^31 - 1 partials");
   *n_out = 0;
   if (n == 0) return GVR_OK;
   cudaStream_t st = (cudaStream_t)stream;
   Partial *d_in = nullptr, *d_out = nullptr;
-  uint64_t *keys = nullptr, *keys_tmp = nullptr;
-  uint32_t *idx = nullptr, *idx_tmp = nullptr, *scratch = nullptr;
-  uint32_t *uniq = nullptr, *multi = nullptr, *upos = nullptr, *mpos = nullptr, *scan_tmp = nullptr;
+  unsigned *mm = nullptr;
+  Arena arena;
+  unsigned hm[2] = {0u, 0u};
+  uint32_t ht[2] = {0u, 0u};
+  uint32_t *totals = nullptr;
   cudaError_t e = cudaSuccess;
   int rc = GVR_OK;
-  uint32_t last[4] = {0, 0, 0, 0};
-  const size_t words = sort_scratch_words(n);
-  const size_t swords = scan_scratch_words(n);
 #define CP_TRY(expr, what)                                        \
   do {                                                            \
     e = (expr);                                                   \
     if (e != cudaSuccess) { rc = cuda_error(e, what); goto done; } \
   } while (0)
   if (location == GVR_MEM_HOST) {
-    CP_TRY(cudaMalloc(&d_in, sizeof(Partial) * n), "cudaMalloc partials");
-    CP_TRY(cudaMalloc(&d_out, sizeof(Partial) * n), "cudaMalloc output");
+    CP_TRY(cudaMallocAsync((void **)&d_in, sizeof(Partial) * n, st), "allocate partials");
+    CP_TRY(cudaMallocAsync((void **)&d_out, sizeof(Partial) * n, st), "allocate output");
     CP_TRY(cudaMemcpyAsync(d_in, partials, sizeof(Partial) * n, cudaMemcpyHostToDevice, st), "copy partials");
   } else {
     d_in = const_cast<Partial *>(partials);
     d_out = out;
   }
-  CP_TRY(cudaMalloc(&keys, sizeof(uint64_t) * n), "cudaMalloc keys");
-  CP_TRY(cudaMalloc(&keys_tmp, sizeof(uint64_t) * n), "cudaMalloc keys");
-  CP_TRY(cudaMalloc(&idx, sizeof(uint32_t) * n), "cudaMalloc index");
-  CP_TRY(cudaMalloc(&idx_tmp, sizeof(uint32_t) * n), "cudaMalloc index");
-  CP_TRY(cudaMalloc(&scratch, sizeof(uint32_t) * words), "cudaMalloc sort scratch");
-  CP_TRY(cudaMalloc(&uniq, sizeof(uint32_t) * n), "cudaMalloc flags");
-  CP_TRY(cudaMalloc(&multi, sizeof(uint32_t) * n), "cudaMalloc flags");
-  CP_TRY(cudaMalloc(&upos, sizeof(uint32_t) * n), "cudaMalloc positions");
-  CP_TRY(cudaMalloc(&mpos, sizeof(uint32_t) * n), "cudaMalloc positions");
-  CP_TRY(cudaMalloc(&scan_tmp, sizeof(uint32_t) * swords), "cudaMalloc scan scratch");
-  key_kernel<<<grid_of(n), 256, 0, st>>>(d_in, n, keys, idx);
+  // pixel-id range (merge computes the same, PartialCompositor.cpp:279-306)
+  CP_TRY(cudaMallocAsync((void **)&mm, 2 * sizeof(unsigned), st), "allocate range");
+  CP_TRY(cudaMemsetAsync(mm, 0xff, sizeof(unsigned), st), "range");
+  CP_TRY(cudaMemsetAsync(mm + 1, 0, sizeof(unsigned), st), "range");
+  range_kernel<<<grid_of(n), 256, 0, st>>>(d_in, n, mm);
   count_launch();
-  CP_TRY(radix_sort_pairs<uint64_t>(keys, idx, keys_tmp, idx_tmp, n, 64, scratch, st), "sort partials");
-  flag_kernel<<<grid_of(n), 256, 0, st>>>(keys, n, uniq, multi);
-  count_launch();
-  CP_TRY(cudaMemcpyAsync(upos, uniq, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st), "copy flags");
-  CP_TRY(cudaMemcpyAsync(mpos, multi, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st), "copy flags");
-  CP_TRY(exclusive_scan(upos, n, scan_tmp, st), "scan");
-  CP_TRY(exclusive_scan(mpos, n, scan_tmp, st), "scan");
-  // totals: last exclusive prefix + last flag
-  CP_TRY(cudaMemcpyAsync(&last[0], upos + n - 1, 4, cudaMemcpyDeviceToHost, st), "read counts");
-  CP_TRY(cudaMemcpyAsync(&last[1], uniq + n - 1, 4, cudaMemcpyDeviceToHost, st), "read counts");
-  CP_TRY(cudaMemcpyAsync(&last[2], mpos + n - 1, 4, cudaMemcpyDeviceToHost, st), "read counts");
-  CP_TRY(cudaMemcpyAsync(&last[3], multi + n - 1, 4, cudaMemcpyDeviceToHost, st), "read counts");
+  CP_TRY(cudaMemcpyAsync(hm, mm, sizeof(hm), cudaMemcpyDeviceToHost, st), "read range");
   CP_TRY(cudaStreamSynchronize(st), "composite");
   {
-    const uint32_t n_unique = last[0] + last[1];
-    const uint32_t n_multi = last[2] + last[3];
-    emit_kernel<<<grid_of(n), 256, 0, st>>>(d_in, keys, idx, n, upos, mpos, uniq, multi, n_unique,
-                                            d_out);
-    count_launch();
-    CP_TRY(cudaGetLastError(), "emit");
-    if (location == GVR_MEM_HOST)
-      CP_TRY(cudaMemcpyAsync(out, d_out, sizeof(Partial) * (n_unique + n_multi), cudaMemcpyDeviceToHost, st),
-             "copy output");
+    const int lo = (int)(hm[0] ^ 0x80000000u), hi = (int)(hm[1] ^ 0x80000000u);
+    const int64_t r = (int64_t)hi - lo + 1;
+    const bool dense = r <= 2 * n + 65536 && r < ((int64_t)1 << 31);
+    const size_t bytes = dense ? dense_bytes(n, r) : sorted_bytes(n);
+    CP_TRY(cudaMallocAsync((void **)&arena.base, bytes, st), "allocate scratch");
+    totals = arena.take<uint32_t>(2);
+    CP_TRY(dense ? composite_dense(d_in, n, lo, r, d_out, arena, totals, st)
+                 : composite_sorted(d_in, n, d_out, arena, totals, st),
+           "composite");
+    CP_TRY(cudaMemcpyAsync(ht, totals, sizeof(ht), cudaMemcpyDeviceToHost, st), "read counts");
     CP_TRY(cudaStreamSynchronize(st), "composite");
-    *n_out = (int64_t)n_unique + n_multi;
+    const int64_t total = (int64_t)ht[0] + ht[1];
+    if (location == GVR_MEM_HOST) {
+      CP_TRY(cudaMemcpyAsync(out, d_out, sizeof(Partial) * total, cudaMemcpyDeviceToHost, st), "copy output");
+      CP_TRY(cudaStreamSynchronize(st), "composite");
+    }
+    *n_out = total;
   }
 done:
 #undef CP_TRY
   if (location == GVR_MEM_HOST) {
-    cudaFree(d_in);
-    cudaFree(d_out);
+    if (d_in) cudaFreeAsync(d_in, st);
+    if (d_out) cudaFreeAsync(d_out, st);
   }
-  cudaFree(keys);
-  cudaFree(keys_tmp);
-  cudaFree(idx);
-  cudaFree(idx_tmp);
-  cudaFree(scratch);
-  cudaFree(uniq);
-  cudaFree(multi);
-  cudaFree(upos);
-  cudaFree(mpos);
-  cudaFree(scan_tmp);
+  if (mm) cudaFreeAsync(mm, st);
+  if (arena.base) cudaFreeAsync(arena.base, st);
   return rc;
 }

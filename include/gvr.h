@@ -367,8 +367,10 @@ typedef struct {
  * without contraction bit for bit.
  *
  * location says where both `partials` and `out` live (GVR_MEM_HOST or
- * GVR_MEM_DEVICE). Scratch is allocated per call (about 40 bytes per
- * record); the call returns after the result is complete. */
+ * GVR_MEM_DEVICE); n < 2^31. Scratch comes from the stream-ordered
+ * allocator (about 24 bytes per record plus 16 per pixel of the id range,
+ * or 56 per record when ids are sparse); the call returns after the result
+ * is complete. */
 GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_partial *out,
                                    int64_t *n_out, int location, void *stream);
 

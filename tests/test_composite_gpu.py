@@ -87,3 +87,17 @@ def test_bad_arguments(comp):
         N.GVR_ERR_INVALID_ARGUMENT
     assert N.lib().gvr_composite_partials(None, 0, None, C.byref(n_out), 7, None) == \
         N.GVR_ERR_INVALID_ARGUMENT
+
+
+def test_sparse_pixel_ids_take_the_sorting_path(comp):
+    """Ids spread over the whole int range (the dense histogram would be too
+    large): same records, same order."""
+    rng = np.random.default_rng(13)
+    a = np.zeros(6000, comp.PARTIAL_DTYPE)
+    ids = rng.integers(-2 ** 31, 2 ** 31 - 1, 1500)
+    a["pixel_id"] = rng.choice(ids, 6000)
+    a["depth"] = rng.uniform(-5, 5, 6000).astype(np.float32)
+    a["alpha"] = rng.uniform(0, 1, 6000).astype(np.float32)
+    a["rgb"] = (rng.uniform(0, 1, (6000, 3)) * a["alpha"][:, None]).astype(np.float32)
+    ims = [a[:2500], a[2500:]]
+    assert comp.PartialCompositor().composite(ims).tobytes() == O.composite_partials_f32(ims).tobytes()
