@@ -149,7 +149,12 @@ _SIGS = {
     "gvr_scene_range": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gvr_render_volume": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams), C.c_void_p,
                                     C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "gvr_scene_update_fields": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_int64, C.c_int, C.c_void_p]),
     "gvr_scene_hex_neighbors": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+    "gvr_render_volume_over": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams),
+                                         C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                         C.POINTER(C.c_uint64)]),
     "gvr_composite_partials": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int64),
                                          C.c_int, C.c_void_p]),
 }

@@ -88,6 +88,35 @@ double piecewise(int n, const double *pos, const double *val, int stride, int c,
   return val[(size_t)lo * stride + c] * (1 - w) + val[(size_t)hi * stride + c] * w;
 }
 
+// Inverse of a row-major 4x4 matrix by Gauss-Jordan elimination with
+// partial pivoting (identity when singular).
+void invert4(const double *m, double *inv)
+{
+  double a[4][8];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 8; ++j) a[i][j] = j < 4 ? m[i * 4 + j] : (j - 4 == i ? 1.0 : 0.0);
+  for (int c = 0; c < 4; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+    if (a[piv][c] == 0.0) {
+      for (int i = 0; i < 16; ++i) inv[i] = (i % 5) == 0 ? 1.0 : 0.0;
+      return;
+    }
+    if (piv != c)
+      for (int j = 0; j < 8; ++j) std::swap(a[c][j], a[piv][j]);
+    const double d = 1.0 / a[c][c];
+    for (int j = 0; j < 8; ++j) a[c][j] *= d;
+    for (int r = 0; r < 4; ++r) {
+      if (r == c) continue;
+      const double f = a[r][c];
+      for (int j = 0; j < 8; ++j) a[r][j] -= f * a[c][j];
+    }
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) inv[i * 4 + j] = a[i][j + 4];
+}
+
 }  // namespace
 
 // Per-view constants of the pinhole model the reference's partials_to_canvas
@@ -145,12 +174,15 @@ void make_view(const gvr_camera &cam, int width, int height, ViewDev *v)
                           {0, ff * z, 0, 0},
                           {0, 0, (fa + n) / (n - fa), 2 * fa * n / (n - fa)},
                           {0, 0, -1, 0}};
+  double M[16];
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) {
       double acc = 0;
       for (int k = 0; k < 4; ++k) acc += P[i][k] * V[k][j];
+      M[i * 4 + j] = acc;
       v->projview[i * 4 + j] = (float)acc;
     }
+  invert4(M, v->inv_projview);
 }
 
 }  // namespace gvr
@@ -362,6 +394,13 @@ int gvr_scene_destroy(gvr_scene *s)
   cudaFree(s->d_batch_depth);
   if (s->batch_exec) cudaGraphExecDestroy(s->batch_exec);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(s->stage[b]);
+    if (s->copied[b]) cudaEventDestroy(s->copied[b]);
+    if (s->consumed[b]) cudaEventDestroy(s->consumed[b]);
+  }
+  cudaFree(s->d_ranges);
   delete s;
   return GVR_OK;
 }
@@ -511,6 +550,116 @@ int gvr_scene_update_field(gvr_scene *s, int domain_id, const void *field, int d
   cudaError_t e = cudaSetDevice(s->device);
   if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
   return upload_field(s, s->domains[domain_id], field, dtype, stride, location);
+}
+
+int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const void *const *fields,
+                            int dtype, int64_t stride, int location, void *stream)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (n < 0 || (n > 0 && (!domain_ids || !fields)))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad domain or field arrays");
+  if (dtype != GVR_DTYPE_FLOAT32 && dtype != GVR_DTYPE_FLOAT64)
+    return set_error(GVR_ERR_UNSUPPORTED, "field dtype must be float32 or float64");
+  if (stride < 1) return set_error(GVR_ERR_INVALID_ARGUMENT, "field stride must be >= 1");
+  if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad field location");
+  for (int k = 0; k < n; ++k) {
+    if (domain_ids[k] < 0 || domain_ids[k] >= (int)s->domains.size())
+      return set_error(GVR_ERR_NOT_FOUND, "no such domain");
+    if (!fields[k]) return set_error(GVR_ERR_INVALID_ARGUMENT, "field is NULL");
+  }
+  if (n == 0) return GVR_OK;
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t esz = dtype == GVR_DTYPE_FLOAT64 ? 8 : 4;
+  auto piped = [&](const Domain &d) {
+    return d.dev.kind != GVR_DOMAIN_HEX && d.dev.assoc == GVR_ASSOC_VERTEX;
+  };
+  auto src_bytes = [&](const Domain &d) {
+    return (size_t)((int64_t)(d.n_values - 1) * stride + 1) * esz;
+  };
+  if (n > s->ranges_cap) {
+    cudaFree(s->d_ranges);
+    s->d_ranges = nullptr;
+    s->ranges_cap = 0;
+    if ((e = cudaMalloc(&s->d_ranges, sizeof(float2) * n)) != cudaSuccess)
+      return cuda_error(e, "cudaMalloc ranges");
+    s->ranges_cap = n;
+  }
+  if (location == GVR_MEM_HOST) {
+    size_t need = 0;
+    for (int k = 0; k < n; ++k)
+      if (piped(s->domains[domain_ids[k]])) need = std::max(need, src_bytes(s->domains[domain_ids[k]]));
+    if (!s->copy_stream) {
+      if ((e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_error(e, "copy stream");
+      for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = cudaEventCreateWithFlags(&s->copied[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->consumed[b], cudaEventDisableTiming);
+      }
+      if (e != cudaSuccess) return cuda_error(e, "copy events");
+    }
+    if (need > s->stage_bytes) {
+      // the old buffers may still be read by bricking from an earlier call
+      if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_error(e, "staging");
+      for (int b = 0; b < 2; ++b) {
+        cudaFree(s->stage[b]);
+        s->stage[b] = nullptr;
+      }
+      s->stage_bytes = 0;
+      for (int b = 0; b < 2; ++b)
+        if ((e = cudaMalloc(&s->stage[b], need)) != cudaSuccess) return cuda_error(e, "staging");
+      s->stage_bytes = need;
+    }
+  }
+  // copies of field j + 1 overlap the bricking of field j
+  int j = 0;
+  for (int k = 0; k < n; ++k) {
+    Domain &d = s->domains[domain_ids[k]];
+    if (!piped(d)) continue;
+    const void *dsrc = fields[k];
+    const int b = j & 1;
+    if (location == GVR_MEM_HOST) {
+      e = cudaStreamWaitEvent(s->copy_stream, s->consumed[b], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->stage[b], fields[k], src_bytes(d), cudaMemcpyHostToDevice, s->copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(s->copied[b], s->copy_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, s->copied[b], 0);
+      if (e != cudaSuccess) return cuda_error(e, "field copy");
+      dsrc = s->stage[b];
+    }
+    e = launch_brick_device(dsrc, dtype, stride, d.dev.dims, d.d_bricks, d.dev.nbrick,
+                            d.d_brick_range, s->d_ranges + k, st);
+    if (e == cudaSuccess && location == GVR_MEM_HOST) e = cudaEventRecord(s->consumed[b], st);
+    if (e != cudaSuccess) return cuda_error(e, "field bricking");
+    ++j;
+  }
+  s->table_dirty = true;
+  s->classify_valid = false;
+  if (j > 0) {
+    std::vector<float2> r((size_t)n);
+    e = cudaMemcpyAsync(r.data(), s->d_ranges, sizeof(float2) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "field ranges");
+    bool bad = false;
+    for (int k = 0; k < n; ++k) {
+      Domain &d = s->domains[domain_ids[k]];
+      if (!piped(d)) continue;
+      d.range[0] = r[k].x;
+      d.range[1] = r[k].y;
+      bad = bad || !(std::isfinite(d.range[0]) && std::isfinite(d.range[1]));
+    }
+    if (bad) return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
+  }
+  // element fields and hexahedral domains: one at a time
+  for (int k = 0; k < n; ++k) {
+    Domain &d = s->domains[domain_ids[k]];
+    if (piped(d)) continue;
+    const int rc = upload_field(s, d, fields[k], dtype, stride, location);
+    if (rc != GVR_OK) return rc;
+  }
+  return GVR_OK;
 }
 
 int gvr_scene_set_batch_granularity(gvr_scene *s, int tiles_per_item)
@@ -697,9 +846,27 @@ static int prepare_march(gvr_scene *s, const gvr_render_params *p, cudaStream_t 
   return GVR_OK;
 }
 
+static int render_one(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
+                      float *rgba, float *depth, int out_location, void *stream,
+                      uint64_t *samples_out, bool over);
+
 int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
                       float *rgba, float *depth, int out_location, void *stream,
                       uint64_t *samples_out)
+{
+  return render_one(s, camera, p, rgba, depth, out_location, stream, samples_out, false);
+}
+
+int gvr_render_volume_over(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
+                           float *rgba, float *depth, int location, void *stream,
+                           uint64_t *samples_out)
+{
+  return render_one(s, camera, p, rgba, depth, location, stream, samples_out, true);
+}
+
+static int render_one(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
+                      float *rgba, float *depth, int out_location, void *stream,
+                      uint64_t *samples_out, bool over)
 {
   if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
   int rc = check_camera(camera);
@@ -726,6 +893,17 @@ int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
   make_view(*camera, p->width, p->height, &view);
   float4 *d_rgba = out_location == GVR_MEM_DEVICE ? (float4 *)rgba : s->d_rgba_tmp;
   float *d_depth = out_location == GVR_MEM_DEVICE ? depth : s->d_depth_tmp;
+  if (over) {
+    // the canvas is read and written in place, one pixel per thread
+    if (out_location == GVR_MEM_HOST) {
+      e = cudaMemcpyAsync(d_rgba, rgba, sizeof(float4) * pixels, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_depth, depth, sizeof(float) * pixels, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return cuda_error(e, "copy canvas to device");
+    }
+    mp.canvas_rgba = d_rgba;
+    mp.canvas_depth = d_depth;
+  }
   e = launch_march(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
                    samples_out ? s->d_counters : nullptr, s->tuning, s->has_hex, st);
   if (e != cudaSuccess) return cuda_error(e, "march kernel launch");

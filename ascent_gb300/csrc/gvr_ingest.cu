@@ -189,6 +189,60 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
   return cudaSuccess;
 }
 
+namespace {
+
+// One block: min and max over the per-brick ranges into *out (NaN when any
+// brick holds a non-finite value).
+__global__ void __launch_bounds__(1024) range_of_bricks_kernel(const float2 *__restrict__ r,
+                                                               int64_t nb, float2 *__restrict__ out)
+{
+  __shared__ float lo_s[32], hi_s[32];
+  __shared__ int bad_s;
+  if (threadIdx.x == 0) bad_s = 0;
+  __syncthreads();
+  float lo = INFINITY, hi = -INFINITY;
+  int bad = 0;
+  for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) {
+    const float2 v = r[i];
+    if (v.x != v.x || v.y != v.y) bad = 1;
+    lo = fminf(lo, v.x);
+    hi = fmaxf(hi, v.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (bad) atomicOr(&bad_s, 1);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    lo_s[w] = lo;
+    hi_s[w] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+      lo = fminf(lo, lo_s[i]);
+      hi = fmaxf(hi, hi_s[i]);
+    }
+    *out = bad_s ? make_float2(NAN, NAN) : make_float2(lo, hi);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
+                                float *d_bricks, const int nbrick[3], float2 *d_brick_range,
+                                float2 *d_range, cudaStream_t stream)
+{
+  const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
+  brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1], dims[2],
+                                                 nbrick[0], nbrick[1], d_bricks, d_brick_range);
+  count_launch();
+  range_of_bricks_kernel<<<1, 1024, 0, stream>>>(d_brick_range, nb, d_range);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, int64_t n, float *d_cells,
                                double range_out[2], Staging &stg, cudaStream_t stream)

@@ -71,6 +71,7 @@ struct ViewDev {
   float xoff;             // pan, in pixels
   float yoff;
   float projview[16];     // row-major projection * view (image depth)
+  double inv_projview[16]; // its inverse (opaque canvas depth -> distance)
 };
 
 struct MarchParams {
@@ -89,6 +90,10 @@ struct MarchParams {
   float early_term;
   float clear_depth;
   float bg[4];
+  // opaque canvas the volume is drawn over (both NULL: a cleared canvas);
+  // rays stop at its depth and partials blend over its colour
+  const float4 *canvas_rgba = nullptr;
+  const float *canvas_depth = nullptr;
 };
 
 // Reusable device buffers of one domain's field uploads: the staging copy
@@ -162,6 +167,15 @@ struct gvr_scene {
   float *d_batch_depth = nullptr;
   int64_t batch_pixels = 0;
   cudaStream_t own_stream = nullptr;
+  // batched field uploads: two staging buffers filled on a copy stream
+  // while the previous field is bricked, per-domain ranges on the device
+  void *stage[2] = {nullptr, nullptr};
+  size_t stage_bytes = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr};
+  cudaEvent_t consumed[2] = {nullptr, nullptr};
+  float2 *d_ranges = nullptr;
+  int ranges_cap = 0;
   cudaGraphExec_t batch_exec = nullptr;
   std::vector<unsigned char> batch_key;
   int batch_graph_builds = 0;
@@ -186,6 +200,11 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
                                Staging &stg, cudaStream_t stream);
+// Brick a vertex field that is already in device memory and reduce its
+// range to *d_range on the device (no host synchronisation).
+cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
+                                float *d_bricks, const int nbrick[3], float2 *d_brick_range,
+                                float2 *d_range, cudaStream_t stream);
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, int64_t n, float *d_cells,
                                double range_out[2], Staging &stg,

@@ -375,6 +375,28 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     r.d[a] = d[a] * inv;
   }
 
+  // Opaque canvas: the ray ends at the world point of the canvas depth
+  // (MapCanvasToRays: pixel (i, j) at depth d unprojected from NDC
+  // (2i/W - 1, 2j/H - 1, 2d - 1); FP64, as in the oracle).
+  float4 cin = make_float4(0.f, 0.f, 0.f, 0.f);
+  float din = mp.clear_depth, t_max = FLT_MAX;
+  if (mp.canvas_depth) {
+    const int64_t pix = (int64_t)py * mp.width + px;
+    cin = mp.canvas_rgba[pix];
+    din = mp.canvas_depth[pix];
+    const double xn = 2.0 * px / mp.width - 1.0, yn = 2.0 * py / mp.height - 1.0;
+    const double zn = 2.0 * (double)din - 1.0;
+    const double *I = view.inv_projview;
+    double P[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) P[q] = I[4 * q] * xn + I[4 * q + 1] * yn + I[4 * q + 2] * zn + I[4 * q + 3];
+    if (P[3] != 0.0) {
+      const double ex = P[0] / P[3] - view.origin[0], ey = P[1] / P[3] - view.origin[1],
+                   ez = P[2] / P[3] - view.origin[2];
+      t_max = (float)sqrt(ex * ex + ey * ey + ez * ez);
+    }
+  }
+
   float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f;
   bool have = false;
   float last_t0 = -FLT_MAX, covered = -FLT_MAX;
@@ -401,6 +423,7 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     last_t0 = bt0;
     last_d = best;
     bt0 = fmaxf(bt0, covered);
+    bt1 = fminf(bt1, t_max);
     covered = fmaxf(covered, bt1);
     const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -426,10 +449,13 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     }
   }
 
-  out = make_float4(0.f, 0.f, 0.f, 0.f);
-  dep = mp.clear_depth;
+  // partials_to_canvas: the composited partial in front of the canvas
+  out = cin;
+  dep = din;
   if (have) {
-    out = make_float4(crgb[0], crgb[1], crgb[2], ca);
+    const float om = 1.f - ca;
+    out = make_float4(crgb[0] + cin.x * om, crgb[1] + cin.y * om, crgb[2] + cin.z * om,
+                      cin.w * om + ca);
     // partials_to_canvas ray rebuild: delta_y runs along ru there
     const float ex = view.dx_scale * (float)(2 * px - mp.width) * 0.5f;
     const float ey = view.dy_scale * (float)(2 * py - mp.height) * 0.5f;

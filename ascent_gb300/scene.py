@@ -140,6 +140,20 @@ class Scene:
         N.call("gvr_scene_update_field", self.handle, int(domain_id), ptr, code, 1, loc)
         del keep
 
+    def update_fields(self, domain_ids, fields, stream=None) -> None:
+        """Replace several domains' fields in one pipelined upload (all numpy
+        on the host, or all torch tensors on one side, same dtype)."""
+        args = [_field_args(f) for f in fields]
+        if len({a[1] for a in args}) > 1 or len({a[3] for a in args}) > 1:
+            raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "fields must share dtype and location")
+        ids = (C.c_int * len(args))(*[int(i) for i in domain_ids])
+        ptrs = (C.c_void_p * len(args))(*[a[0].value for a in args])
+        code = args[0][1] if args else N.DTYPE_FLOAT32
+        loc = args[0][3] if args else N.MEM_HOST
+        st = None if stream is None else C.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+        N.call("gvr_scene_update_fields", self.handle, len(args), ids, ptrs, code, 1, loc, st)
+        del args
+
     def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4) -> None:
         """Launch shape of the march kernel; images do not depend on it."""
         N.call("gvr_scene_set_tuning", self.handle, int(packet_w), int(unroll), int(min_blocks))
@@ -181,6 +195,34 @@ class Scene:
             depth = np.empty((h, w), dtype=np.float32)
             N.call("gvr_render_volume", self.handle, C.byref(camera), C.byref(params),
                    C.c_void_p(rgba.ctypes.data), C.c_void_p(depth.ctypes.data), N.MEM_HOST, st, nptr)
+        if count_samples:
+            return rgba, depth, int(n.value)
+        return rgba, depth
+
+    def render_over(self, camera: N.Camera, params: N.RenderParams, canvas_rgba, canvas_depth, *,
+                    count_samples=False):
+        """Render the volume over an opaque canvas: canvas_rgba (H, W, 4) and
+        canvas_depth (H, W, image depth, 1 = empty) as numpy arrays (host) or
+        torch CUDA tensors (updated in place). Returns (rgba, depth)."""
+        n = C.c_uint64(0)
+        nptr = C.byref(n) if count_samples else None
+        try:
+            import torch
+            on_device = isinstance(canvas_rgba, torch.Tensor) and canvas_rgba.is_cuda
+        except ImportError:  # pragma: no cover
+            on_device = False
+        if on_device:
+            rgba, depth = canvas_rgba, canvas_depth
+            if not (rgba.is_contiguous() and depth.is_contiguous()):
+                raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "canvas tensors must be contiguous")
+            st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            N.call("gvr_render_volume_over", self.handle, C.byref(camera), C.byref(params),
+                   C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, st, nptr)
+        else:
+            rgba = np.array(canvas_rgba, dtype=np.float32, copy=True, order="C")
+            depth = np.array(canvas_depth, dtype=np.float32, copy=True, order="C")
+            N.call("gvr_render_volume_over", self.handle, C.byref(camera), C.byref(params),
+                   C.c_void_p(rgba.ctypes.data), C.c_void_p(depth.ctypes.data), N.MEM_HOST, None, nptr)
         if count_samples:
             return rgba, depth, int(n.value)
         return rgba, depth

@@ -245,6 +245,18 @@ GVR_API int gvr_scene_hex_locate(gvr_scene *scene, int domain_id, const float *p
 GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *field,
                            int dtype, int64_t stride, int location);
 
+/* Replace the fields of n domains in one call (each as
+ * gvr_scene_update_field would, same dtype/stride/location for all) — the
+ * per-domain AddField loop of the Blueprint adapter when a simulation
+ * publishes a new time step (ascent_vtkh_data_adapter.cpp:1782-2040). Host
+ * fields are copied through two staging buffers on a copy stream while the
+ * previous domain is bricked on `stream`; ranges are reduced on the device
+ * and read back once. Host fields in pinned memory overlap best. Returns
+ * after the uploads are complete. */
+GVR_API int gvr_scene_update_fields(gvr_scene *scene, int n, const int *domain_ids,
+                                    const void *const *fields, int dtype, int64_t stride,
+                                    int location, void *stream);
+
 GVR_API int gvr_scene_num_domains(const gvr_scene *scene, int *n);
 
 /* Launch shape of the scene's march kernel: pixel packet width per warp
@@ -280,6 +292,20 @@ GVR_API int gvr_render_volume(gvr_scene *scene, const gvr_camera *camera,
                       const gvr_render_params *params, float *rgba,
                       float *depth, int out_location, void *stream,
                       uint64_t *samples_out);
+
+/* Render the volume over an opaque canvas: rgba and depth (in `location`
+ * memory) hold on entry the colours and image-space depths (0.5 z_ndc + 0.5,
+ * 1 = nothing drawn) that the scene's opaque plots left, and on return the
+ * canvas with the volume composited in front. Each ray stops where the
+ * canvas depth unprojects to (the ray's MaxDistance after
+ * RayOperations::MapCanvasToRays, VolumeRenderer.cpp:243-247); partials
+ * blend over the canvas colour as partials_to_canvas does
+ * (VolumeRenderer.cpp:366-385); pixels no partial reaches keep the canvas.
+ * This is the volume pass of a mixed scene after vtkh::Scene::Render's
+ * opaque pass (Scene.cpp:154-212). */
+GVR_API int gvr_render_volume_over(gvr_scene *scene, const gvr_camera *camera,
+                                   const gvr_render_params *params, float *rgba, float *depth,
+                                   int location, void *stream, uint64_t *samples_out);
 
 /* Render n_views cameras of the scene in one persistent launch: rgba holds
  * n_views images of 4*W*H floats and depth n_views images of W*H floats,

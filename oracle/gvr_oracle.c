@@ -1021,19 +1021,73 @@ static int cmp_rpartial(const void *pa, const void *pb)
   return a->dom - b->dom;
 }
 
+/* Inverse of a row-major 4x4 matrix (Gauss-Jordan, partial pivoting);
+ * identity when singular. */
+static void invert4(const double M[4][4], double I[4][4])
+{
+  double a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? M[r][c] : (c - 4 == r ? 1.0 : 0.0);
+  for (int c = 0; c < 4; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
+    if (a[piv][c] == 0.0) {
+      for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) I[r][k] = r == k;
+      return;
+    }
+    for (int k = 0; k < 8; ++k) { double t = a[c][k]; a[c][k] = a[piv][k]; a[piv][k] = t; }
+    double d = 1.0 / a[c][c];
+    for (int k = 0; k < 8; ++k) a[c][k] *= d;
+    for (int r = 0; r < 4; ++r) {
+      if (r == c) continue;
+      double f = a[r][c];
+      for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int k = 0; k < 4; ++k) I[r][k] = a[r][k + 4];
+}
+
+static int render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
+                       int row0, int row1, float *rgba, float *depth, int over,
+                       uint64_t *samples_out);
+
 /* Render image rows [row0, row1) of the scene for one camera into full-size
  * buffers (rgba: 4*W*H floats, depth: W*H floats; other rows untouched).
  * *samples_out (if non-NULL) receives the number of samples taken. */
 int or_render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
                    int row0, int row1, float *rgba, float *depth, uint64_t *samples_out)
 {
+  return render_rows(s, cam, p, row0, row1, rgba, depth, 0, samples_out);
+}
+
+/* Render over an opaque canvas held in rgba/depth (image depth 0.5 z + 0.5,
+ * 1 = empty): every ray ends at the world point its pixel's canvas depth
+ * unprojects to (assumption A11: pixel (i, j) at NDC (2i/W - 1, 2j/H - 1,
+ * 2d - 1) through the inverse projection * view, the distance from the
+ * camera becomes the ray's MaxDistance as in RayOperations::MapCanvasToRays,
+ * VolumeRenderer.cpp:243-247), and partials blend over the canvas colour
+ * (partials_to_canvas, VolumeRenderer.cpp:366-385). */
+int or_render_over(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
+                   float *rgba, float *depth, uint64_t *samples_out)
+{
+  return render_rows(s, cam, p, 0, p->height, rgba, depth, 1, samples_out);
+}
+
+static int render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_params *p,
+                       int row0, int row1, float *rgba, float *depth, int over,
+                       uint64_t *samples_out)
+{
   const int W = p->width, H = p->height;
   if (W < 1 || H < 1 || !p->lut_rgba || p->lut_size < 2) return GVR_ERR_INVALID_ARGUMENT;
   if (row0 < 0) row0 = 0;
   if (row1 > H) row1 = H;
   or_basis b = make_basis(cam, W, H);
-  double M[4][4];
+  double M[4][4], IM[4][4];
   projview(cam, W, H, M);
+  invert4(M, IM);
   const int nd = s->n;
   uint64_t total = 0;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
@@ -1056,6 +1110,21 @@ int or_render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_pa
         }
       }
       qsort(parts, np, sizeof(or_rpartial), cmp_rpartial);
+      const int64_t pix = (int64_t)j * W + i;
+      REAL cin[4] = {0, 0, 0, 0};
+      REAL din = (REAL)p->clear_depth;
+      REAL t_max = INFINITY;
+      if (over) {
+        for (int c = 0; c < 4; ++c) cin[c] = rgba[pix * 4 + c];
+        din = depth[pix];
+        double q[4] = {2.0 * i / W - 1.0, 2.0 * j / H - 1.0, 2.0 * (double)depth[pix] - 1.0, 1.0}, P[4];
+        for (int r = 0; r < 4; ++r)
+          P[r] = IM[r][0] * q[0] + IM[r][1] * q[1] + IM[r][2] * q[2] + IM[r][3] * q[3];
+        if (P[3] != 0.0) {
+          double ex = P[0] / P[3] - b.origin.x, ey = P[1] / P[3] - b.origin.y, ez = P[2] / P[3] - b.origin.z;
+          t_max = (REAL)(float)sqrt(ex * ex + ey * ey + ez * ez);
+        }
+      }
       REAL rgb[3] = {0, 0, 0}, a = 0, front_depth = 0;
       int have = 0;
       REAL covered = -INFINITY;
@@ -1065,6 +1134,7 @@ int or_render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_pa
         /* A7: domains in entry order, each marched from the furthest exit
          * reached so far */
         if (t0 < covered) t0 = covered;
+        if (t1 > t_max) t1 = t_max;
         if (t1 > covered) covered = t1;
         if (p->early_term < 1 && a >= (REAL)p->early_term) break;
         total += (uint64_t)march(&s->d[parts[k].dom], b.origin, dir, t0, t1, p, a, acc);
@@ -1078,12 +1148,13 @@ int or_render_rows(const or_scene *s, const gvr_camera *cam, const gvr_render_pa
           blend_partial(rgb, &a, acc, acc[3]);
         }
       }
-      const int64_t pix = (int64_t)j * W + i;
-      REAL out[4] = {0, 0, 0, 0};
-      REAL dep = (REAL)p->clear_depth;
+      REAL out[4] = {cin[0], cin[1], cin[2], cin[3]};
+      REAL dep = din;
       if (have) {
-        /* canvas was cleared to transparent: colour + 0 * (1 - alpha) */
-        out[0] = rgb[0]; out[1] = rgb[1]; out[2] = rgb[2]; out[3] = a;
+        /* composited partial in front of the canvas (a cleared canvas is 0) */
+        REAL om = 1 - a;
+        out[0] = rgb[0] + cin[0] * om; out[1] = rgb[1] + cin[1] * om;
+        out[2] = rgb[2] + cin[2] * om; out[3] = cin[3] * om + a;
         dep = image_depth(&b, M, W, H, i, j, front_depth);
       }
       if (p->quantize_uint8) {

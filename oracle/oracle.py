@@ -69,6 +69,7 @@ def load(precision: int = 64) -> C.CDLL:
     lib.or_hex_locate.argtypes = [vp, i, P(f), i, P(i), P(f)]
     lib.or_render.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
     lib.or_render_rows.argtypes = [vp, P(Camera), P(RenderParams), i, i, P(f), P(f), P(C.c_uint64)]
+    lib.or_render_over.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
     lib.or_num_threads.restype = i
     _libs[precision] = lib
     return lib
@@ -151,6 +152,17 @@ class OracleScene:
         n = C.c_uint64(0)
         rc = self.lib.or_render(self.handle, C.byref(cam), C.byref(params), fptr(rgba), fptr(depth),
                                 C.byref(n))
+        if rc != 0:
+            raise RuntimeError(f"oracle render failed with status {rc}")
+        return rgba, depth, int(n.value)
+
+    def render_over(self, cam: Camera, params: RenderParams, canvas_rgba, canvas_depth):
+        """Render over an opaque canvas (copies of the inputs are returned)."""
+        rgba = np.array(canvas_rgba, dtype=np.float32, copy=True, order="C")
+        depth = np.array(canvas_depth, dtype=np.float32, copy=True, order="C")
+        n = C.c_uint64(0)
+        rc = self.lib.or_render_over(self.handle, C.byref(cam), C.byref(params), fptr(rgba), fptr(depth),
+                                     C.byref(n))
         if rc != 0:
             raise RuntimeError(f"oracle render failed with status {rc}")
         return rgba, depth, int(n.value)
