@@ -124,9 +124,25 @@ __global__ void range_kernel(const Partial *__restrict__ in, int64_t n, unsigned
   }
   lo = __reduce_min_sync(0xffffffffu, lo);
   hi = __reduce_max_sync(0xffffffffu, hi);
+  // one pair of atomics per block, not per warp (thousands of warps on two
+  // addresses serialise at L2)
+  __shared__ unsigned slo[32], shi[32];
+  const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    atomicMin(mm, lo);
-    atomicMax(mm + 1, hi);
+    slo[w] = lo;
+    shi[w] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (int)(blockDim.x >> 5);
+    lo = threadIdx.x < nw ? slo[threadIdx.x] : 0xffffffffu;
+    hi = threadIdx.x < nw ? shi[threadIdx.x] : 0u;
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (threadIdx.x == 0) {
+      atomicMin(mm, lo);
+      atomicMax(mm + 1, hi);
+    }
   }
 }
 
