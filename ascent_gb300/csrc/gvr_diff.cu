@@ -27,7 +27,8 @@
 // per CTA; field gradients are
 // summed per ray while consecutive samples stay in one cell, then combined
 // with the neighbouring lane's sums when both leave the same cell at the
-// same step, and added to the eight corners with one atomic per node.
+// same step, and added with two float4 atomics per cell into a corner-quad
+// buffer that is folded into the node gradient at the end.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -200,11 +201,14 @@ diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews 
 // Add g8 (the gradients of one cell's eight corners) to the field gradient.
 // Warp-aggregated in pairs: lanes 2i and 2i + 1 (neighbouring pixels in x)
 // that flush the same cell at the same step add their sums first, so one
-// atomic per corner covers both. Measured against pooling whole peer sets
+// atomic covers both. Measured against pooling whole peer sets
 // (__match_any_sync, then shuffles) and against 2x2 / 4x2 pixel groups,
 // pairs were fastest: wider groups cost more shuffles than they save
-// atomics. Called by all lanes of the warp.
-__device__ __forceinline__ void flush_cell(float *__restrict__ gfield, const DiffGrid &g,
+// atomics. The sums go to the corner-quad buffer gq (one float4 per cell
+// base: corners (x, y), (x+1, y), (x, y+1), (x+1, y+1) of one z layer), so a
+// flush is two 16-byte vector atomics, each in one sector; fold_quads adds
+// the quads into the node gradient afterwards. Called by all lanes.
+__device__ __forceinline__ void flush_cell(float4 *__restrict__ gq, const DiffGrid &g,
                                            int64_t base, const float g8[8], bool active)
 {
   const int lane = threadIdx.x & 31;
@@ -217,11 +221,26 @@ __device__ __forceinline__ void flush_cell(float *__restrict__ gfield, const Dif
     s[m] = g8[m] + (pair ? x : 0.f);
   }
   if (!active || (pair && (lane & 1))) return;
-  const int64_t sy = g.dims[0], sz = (int64_t)g.dims[0] * g.dims[1];
-  const int64_t off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
-#pragma unroll
-  for (int m = 0; m < 8; ++m)
-    if (s[m] != 0.f) atomicAdd(gfield + base + off[m], s[m]);
+  const int64_t sz = (int64_t)g.dims[0] * g.dims[1];
+  atomicAdd(gq + base, make_float4(s[0], s[1], s[2], s[3]));
+  atomicAdd(gq + base + sz, make_float4(s[4], s[5], s[6], s[7]));
+}
+
+// grad[i] += quads whose corners include node i: its own quad's (x, y)
+// entry, the (x+1, y) entry of the quad to its left, and so on.
+__global__ void fold_quads(const float4 *__restrict__ gq, const DiffGrid g,
+                           float *__restrict__ grad)
+{
+  const int64_t nx = g.dims[0], ny = g.dims[1], n = nx * ny * g.dims[2];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = i % nx, y = (i / nx) % ny;
+    float acc = gq[i].x;
+    if (x > 0) acc += gq[i - 1].y;
+    if (y > 0) acc += gq[i - nx].z;
+    if (x > 0 && y > 0) acc += gq[i - nx - 1].w;
+    if (acc != 0.f) grad[i] += acc;
+  }
 }
 
 // Add the register sums of LUT interval li (entries li and li + 1) to a
@@ -242,7 +261,7 @@ __global__ void __launch_bounds__(256)
 diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews views,
               const DiffParams p, const float4 *__restrict__ g_lut,
               const float4 *__restrict__ grad_rgba, const float *__restrict__ ws,
-              float *__restrict__ gfield, float *__restrict__ glut)
+              float4 *__restrict__ gq, float *__restrict__ glut)
 {
   extern __shared__ float4 smem[];
   float4 *lut = smem;
@@ -370,7 +389,7 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
         }
         // pool the field gradient per cell; flush when a lane changes cell
         const bool change = on && base != cur && cur >= 0;
-        flush_cell(gfield, g, cur, g8, change);
+        flush_cell(gq, g, cur, g8, change);
         if (change) {
 #pragma unroll
           for (int m = 0; m < 8; ++m) g8[m] = 0.f;
@@ -390,7 +409,7 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
       }
     }
   }
-  flush_cell(gfield, g, cur, g8, cur >= 0);
+  flush_cell(gq, g, cur, g8, cur >= 0);
   flush_lut(slg + (lane & (nc - 1)) * cstride, 1, li, lg);
   __syncthreads();
   for (int i = threadIdx.x; i < 4 * p.lut_size; i += blockDim.x)
@@ -506,12 +525,24 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
-  dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
-  diff_backward<<<grid, 256, smem, (cudaStream_t)stream>>>(
-      field, g, views, p, (const float4 *)lut, (const float4 *)grad_rgba,
-      workspace, grad_field, grad_lut);
-  count_launch();
-  e = cudaGetLastError();
+  // corner-quad buffer of the field gradient, from the stream-ordered pool
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t nodes = (int64_t)g.dims[0] * g.dims[1] * g.dims[2];
+  float4 *gq = nullptr;
+  e = cudaMallocAsync((void **)&gq, sizeof(float4) * nodes, st);
+  if (e != cudaSuccess) return cuda_error(e, "allocate gradient quads");
+  e = cudaMemsetAsync(gq, 0, sizeof(float4) * nodes, st);
+  if (e == cudaSuccess) {
+    dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
+    diff_backward<<<grid, 256, smem, st>>>(field, g, views, p, (const float4 *)lut,
+                                           (const float4 *)grad_rgba, workspace, gq, grad_lut);
+    count_launch();
+    fold_quads<<<(unsigned)std::min<int64_t>((nodes + 255) / 256, 152 * 16), 256, 0, st>>>(gq, g,
+                                                                                         grad_field);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(gq, st);
   if (e != cudaSuccess) return cuda_error(e, "differentiable backward launch");
   return GVR_OK;
 }
