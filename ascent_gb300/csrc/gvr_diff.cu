@@ -21,10 +21,9 @@
 //   dL/da_k = T_k (g_rgb . (c_k - R'_k) + g_A (1 - A'_k)),
 //   R'_{k-1} = a_k c_k + (1 - a_k) R'_k,  A'_{k-1} = a_k + (1 - a_k) A'_k.
 // LUT gradients are summed in registers while consecutive samples of a ray
-// stay in one LUT interval, then added to one of up to 16 private
-// shared-memory copies per CTA (lane l uses copy l % 16, so neighbouring
-// rays that hit the same entry do not serialise on one address), summed once
-// per CTA; field gradients are
+// stay in one LUT interval, then added with two float4 atomics to the CTA's
+// private copy in global memory; a last kernel sums the copies. Field
+// gradients are
 // summed per ray while consecutive samples stay in one cell, then combined
 // with the neighbouring lane's sums when both leave the same cell at the
 // same step, and added with two float4 atomics per cell into a corner-quad
@@ -61,8 +60,8 @@ struct DiffParams {
   int height;
   int n_views;
   int lut_size;
-  int lut_copies;  // private LUT-gradient copies per CTA (backward)
   int n_seg;       // checkpoint segments per ray
+  int lut_copies;  // backward: LUT-gradient copies in global memory (CTA c uses c % copies)
   int64_t n_rays;  // views x height x width
   int64_t v_offset;  // start of the per-sample scalar cache in the workspace
   float sample_dist;
@@ -243,44 +242,38 @@ __global__ void fold_quads(const float4 *__restrict__ gq, const DiffGrid g,
   }
 }
 
-// Add the register sums of LUT interval li (entries li and li + 1) to a
-// shared-memory copy of the LUT gradient (floats `stride` apart) and clear
-// them.
-__device__ __forceinline__ void flush_lut(float *copy, int stride, int li, float (&lg)[8])
+// Add the register sums of LUT interval li (entries li and li + 1) to this
+// CTA's LUT-gradient copy as two float4 atomics, and clear them.
+__device__ __forceinline__ void flush_lut4(float *copy, int li, float (&lg)[8])
 {
   if (li < 0) return;
-  float *q = copy + 4 * li * stride;
+  float4 *q = reinterpret_cast<float4 *>(copy + 4 * li);
+  atomicAdd(q, make_float4(lg[0], lg[1], lg[2], lg[3]));
+  atomicAdd(q + 1, make_float4(lg[4], lg[5], lg[6], lg[7]));
 #pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    if (lg[m] != 0.f) atomicAdd(q + m * stride, lg[m]);
-    lg[m] = 0.f;
-  }
+  for (int m = 0; m < 8; ++m) lg[m] = 0.f;
 }
 
 __global__ void __launch_bounds__(256)
 diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews views,
               const DiffParams p, const float4 *__restrict__ g_lut,
               const float4 *__restrict__ grad_rgba, const float *__restrict__ ws,
-              float4 *__restrict__ gq, float *__restrict__ glut)
+              float4 *__restrict__ gq, float *__restrict__ glut_cta)
 {
   extern __shared__ float4 smem[];
   float4 *lut = smem;
-  // LUT gradient: p.lut_copies (a power of two <= 16) private copies of
-  // 4 * lut_size floats, one float of padding apart so that equal entries of
-  // different copies sit in different banks; lane l adds into copy
-  // l % copies, so the lanes of a warp that hit the same entry mostly hit
-  // different addresses. (Interleaving the copies float by float bounds bank
-  // conflicts at two lanes but measured slower: lanes l and l + 16 then
-  // collide on one address whenever they hit the same entry.)
+  // LUT gradient: this CTA's private copy in global memory (L2-resident),
+  // two float4 atomics per flushed interval. Measured against 16 padded
+  // private copies in shared memory per CTA (8 scalar shared atomics per
+  // flush, bank conflicts, 64 KB of shared memory taken from L1): 4.72 vs
+  // 5.86 ms for the whole training step.
   float *lut_a = reinterpret_cast<float *>(smem + p.lut_size);  // opacity column
-  float *slg = lut_a + p.lut_size;
-  const int nc = p.lut_copies;
-  const int cstride = 4 * p.lut_size + 1;
+  const int64_t cta = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  float *slg = glut_cta + (cta % p.lut_copies) * 4 * p.lut_size;
   for (int i = threadIdx.x; i < p.lut_size; i += blockDim.x) {
     lut[i] = g_lut[i];
     lut_a[i] = g_lut[i].w;
   }
-  for (int i = threadIdx.x; i < cstride * nc; i += blockDim.x) slg[i] = 0.f;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -367,7 +360,7 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
           // transfer-function entries i0 and i0 + 1: summed in registers
           // while consecutive samples stay in one LUT interval
           if (i0 != li) {
-            flush_lut(slg + (lane & (nc - 1)) * cstride, 1, li, lg);
+            flush_lut4(slg, li, lg);
             li = i0;
           }
           const float w0 = 1.f - wl;
@@ -410,14 +403,19 @@ diff_backward(const float *__restrict__ field, const DiffGrid g, const DiffViews
     }
   }
   flush_cell(gq, g, cur, g8, cur >= 0);
-  flush_lut(slg + (lane & (nc - 1)) * cstride, 1, li, lg);
-  __syncthreads();
-  for (int i = threadIdx.x; i < 4 * p.lut_size; i += blockDim.x)
-  {
-    float acc = 0.f;
-    for (int c = 0; c < nc; ++c) acc += slg[c * cstride + i];
-    if (acc != 0.f) atomicAdd(glut + i, acc);
-  }
+  flush_lut4(slg, li, lg);
+}
+
+// glut[i] += the CTAs' private LUT-gradient copies, 32 CTAs per thread
+__global__ void sum_lut_copies(const float *__restrict__ glut_cta, int64_t n_cta, int n,
+                               float *__restrict__ glut)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t c0 = (int64_t)blockIdx.y * 32, c1 = min(c0 + 32, n_cta);
+  float acc = 0.f;
+  for (int64_t c = c0; c < c1; ++c) acc += glut_cta[c * n + i];
+  if (acc != 0.f) atomicAdd(glut + i, acc);
 }
 
 int diff_setup(const float *field, const int dims[3], const double origin[3],
@@ -448,13 +446,13 @@ int diff_setup(const float *field, const int dims[3], const double origin[3],
   p.height = params->height;
   p.n_views = n_views;
   p.lut_size = params->lut_size;
-  p.lut_copies = 1;
   p.sample_dist = params->sample_dist;
   p.scalar_min = params->scalar_min;
   p.inv_range = params->scalar_max > params->scalar_min
                     ? 1.f / (params->scalar_max - params->scalar_min) : 0.f;
   const double max_samples = std::sqrt(diag) / params->sample_dist + 2.0;
   p.n_seg = (int)((max_samples + kDiffK - 1) / kDiffK);
+  p.lut_copies = 1;
   p.n_rays = (int64_t)n_views * params->width * params->height;
   p.v_offset = p.n_rays * p.n_seg;
   return GVR_OK;
@@ -517,11 +515,7 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   if (rc != GVR_OK) return rc;
   if (!lut || !grad_rgba || !workspace || !grad_field || !grad_lut)
     return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL buffer");
-  // up to 16 private LUT-gradient copies within ~72 KB of shared memory
-  const size_t per_copy = sizeof(float) * (4 * (size_t)p.lut_size + 1);
-  p.lut_copies = 16;
-  while (p.lut_copies > 1 && per_copy * p.lut_copies > (72u << 10)) p.lut_copies >>= 1;
-  const size_t smem = (sizeof(float4) + sizeof(float)) * p.lut_size + per_copy * p.lut_copies;
+  const size_t smem = (sizeof(float4) + sizeof(float)) * p.lut_size;
   cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
@@ -529,13 +523,23 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t nodes = (int64_t)g.dims[0] * g.dims[1] * g.dims[2];
   float4 *gq = nullptr;
+  dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
+  const int64_t n_cta = (int64_t)grid.x * grid.y * grid.z;
+  // one copy per CTA, at most 512 MB of copies (CTAs then share them)
+  p.lut_copies = (int)std::max<int64_t>(
+      1, std::min<int64_t>(n_cta, ((int64_t)512 << 20) / (16 * (int64_t)p.lut_size)));
+  float *glc = nullptr;
   e = cudaMallocAsync((void **)&gq, sizeof(float4) * nodes, st);
   if (e != cudaSuccess) return cuda_error(e, "allocate gradient quads");
-  e = cudaMemsetAsync(gq, 0, sizeof(float4) * nodes, st);
+  e = cudaMallocAsync((void **)&glc, sizeof(float) * 4 * p.lut_size * p.lut_copies, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(glc, 0, sizeof(float) * 4 * p.lut_size * p.lut_copies, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(gq, 0, sizeof(float4) * nodes, st);
   if (e == cudaSuccess) {
-    dim3 grid((p.width + 15) / 16, (p.height + 15) / 16, n_views);
     diff_backward<<<grid, 256, smem, st>>>(field, g, views, p, (const float4 *)lut,
-                                           (const float4 *)grad_rgba, workspace, gq, grad_lut);
+                                           (const float4 *)grad_rgba, workspace, gq, glc);
+    count_launch();
+    sum_lut_copies<<<dim3((4 * p.lut_size + 255) / 256, (unsigned)((p.lut_copies + 31) / 32)), 256, 0,
+                     st>>>(glc, p.lut_copies, 4 * p.lut_size, grad_lut);
     count_launch();
     fold_quads<<<(unsigned)std::min<int64_t>((nodes + 255) / 256, 152 * 16), 256, 0, st>>>(gq, g,
                                                                                          grad_field);
@@ -543,6 +547,7 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
     e = cudaGetLastError();
   }
   cudaFreeAsync(gq, st);
+  if (glc) cudaFreeAsync(glc, st);
   if (e != cudaSuccess) return cuda_error(e, "differentiable backward launch");
   return GVR_OK;
 }
