@@ -631,6 +631,10 @@ MarchFn select(const Tuning &t, bool has_hex)
 {
   // the hex path keeps eight corner records in registers: 2 CTAs per SM
   if (has_hex) return t.packet_w == 4 ? march_kernel<4, 1, 2, true> : march_kernel<8, 1, 2, true>;
+  // three samples per iteration exists only at 4 CTAs per SM (at 3 it
+  // measured slower than two)
+  if (t.unroll >= 3)
+    return t.packet_w == 4 ? pick<4, 3, 4>() : (t.packet_w == 16 ? pick<16, 3, 4>() : pick<8, 3, 4>());
   const int u = t.unroll >= 2 ? 2 : 1;
   const int m = t.min_blocks >= 4 ? 4 : 3;
   switch (t.packet_w) {

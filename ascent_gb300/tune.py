@@ -19,8 +19,11 @@ from pathlib import Path
 
 from . import _native as N
 
-CANDIDATES = [dict(packet_w=p, unroll=u, min_blocks=m)
-              for p, u, m in itertools.product((8, 4, 16), (2, 1), (3, 4))]
+CANDIDATES = ([dict(packet_w=p, unroll=u, min_blocks=m)
+               for p, u, m in itertools.product((8, 4, 16), (2, 1), (3, 4))] +
+              [dict(packet_w=p, unroll=3, min_blocks=4) for p in (8, 4, 16)])
+# the batch kernel has no 3-sample variant (it would run as 2)
+BATCH_CANDIDATES = [c for c in CANDIDATES if c["unroll"] != 3]
 CACHE = Path(os.environ.get("GVR_TUNE_CACHE", Path.home() / ".cache" / "gvr_tune.json"))
 
 
@@ -61,7 +64,7 @@ def autotune_batch(scene, cameras, params, reps: int = 2) -> dict:
            torch.empty((v, params.height, params.width), dtype=torch.float32, device=dev))
     stream = torch.cuda.current_stream(scene.device)
     results = {}
-    for cand in CANDIDATES:
+    for cand in BATCH_CANDIDATES:
         for g in GRANULARITY:
             scene.set_tuning(**cand)
             scene.set_batch_granularity(g)
