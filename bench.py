@@ -162,7 +162,10 @@ def cpu_sample(wl, cam, params, seconds: float, per_step: bool = False):
     from oracle import oracle as O
     osc = O.OracleScene(32)
     for d in wl.domains:
-        osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+        if hasattr(d, "conn"):
+            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
+        else:
+            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
     h, w = params.height, params.width
     rgba = np.zeros((h, w, 4), np.float32)
     depth = np.zeros((h, w), np.float32)
@@ -231,9 +234,12 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
     alg = n * 160 + size * size * BYTES_PER_PIXEL
     sc.close()
     acc = accuracy(dev, wl, [cam], p, rows=(size // 2 - 8, size // 2 + 8))
+    cpu, _ = cpu_sample(wl, cam, p, 5.0)
     return {"workload": wl.name, "cells": n_cells ** 3, "samples_per_frame": n,
             "error_vs_fp64_oracle": acc,
             "gsamples_per_s": n / ms / 1e6, "fps": 1e3 / ms, "ms_per_frame": ms,
+            "cpu_port_gsamples_per_s": cpu["value"], "cpu_cores": cpu["cores"],
+            "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
             "bvh_build_ms": build_ms, "face_neighbour_build_ms": nbr_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
             "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": pk["hbm_gbs"],
                          "unit": "GB/s", "frac": alg / ms / 1e6 / pk["hbm_gbs"],
@@ -282,7 +288,11 @@ def bench_batch(dev, reps=5):
     builds = sc.batch_graph_builds
     sc.close()
     acc = accuracy(dev, wl, [cams[0], cams[27]], p, rows=(h // 2 - 32, h // 2 + 32))
+    cpu, _ = cpu_sample(wl, cams[0], p, 5.0)
+    cpu_images = cpu["value"] * 1e9 / (n / v)
     return {"workload": wl.name, "domains": len(wl.domains), "views": v, "image": [w, h],
+            "cpu_port_images_per_s": cpu_images, "cpu_cores": cpu["cores"],
+            "speedup_vs_cpu_port": v * 1e3 / batch_ms / cpu_images,
             "samples_per_batch": n, "per_view_loop_ms": loop_ms, "batched_ms": batch_ms,
             "per_view_loop_images_per_s": v * 1e3 / loop_ms, "batched_images_per_s": v * 1e3 / batch_ms,
             "speedup": loop_ms / batch_ms, "batched_gsamples_per_s": n / batch_ms / 1e6,
@@ -478,7 +488,10 @@ def run_reference(args):
     from oracle import oracle as O
     osc = O.OracleScene(32)
     for d in wl.domains:
-        osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+        if hasattr(d, "conn"):
+            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
+        else:
+            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
     h, w = params.height, params.width
     rgba = np.zeros((h, w, 4), np.float32)
     depth = np.zeros((h, w), np.float32)
