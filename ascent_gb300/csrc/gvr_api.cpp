@@ -430,6 +430,7 @@ static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, i
                            d.d_cells, d.range, d.stg, 0);
   }
   if (e != cudaSuccess) return cuda_error(e, "field upload");
+  if (ingest_timed_out()) return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
   if (!(std::isfinite(d.range[0]) && std::isfinite(d.range[1])))
     return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
   s->table_dirty = true;
@@ -642,6 +643,7 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
     e = cudaMemcpyAsync(r.data(), s->d_ranges, sizeof(float2) * n, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "field ranges");
+    if (ingest_timed_out()) return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
     bool bad = false;
     for (int k = 0; k < n; ++k) {
       Domain &d = s->domains[domain_ids[k]];

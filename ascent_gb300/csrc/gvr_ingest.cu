@@ -7,6 +7,7 @@
 // renderer's own: 8^3-cell bricks with a one-node apron plus a per-brick
 // {min,max} macrocell grid used for empty-space skipping.
 #include <cfloat>
+#include <cstdint>
 #include <cstdio>
 
 #include "gvr_internal.h"
@@ -68,6 +69,185 @@ brick_kernel(const void *__restrict__ src, int dtype, int64_t stride, int nx,
     }
     brick_range[b] = bad ? make_float2(NAN, NAN) : make_float2(vmin, vmax);
   }
+}
+
+// ---------------------------------------------------------------------
+// Staged bricking of contiguous float32 fields. A CTA builds a run of up to
+// 8 bricks along x: one thread issues a bulk copy (cp.async.bulk, completing
+// on an mbarrier) of each of the run's 81 node rows (9 y x 9 z, ~65 floats
+// each) into shared memory, then each warp writes one brick from there with
+// coalesced stores and reduces its min/max. The per-brick kernel above reads
+// the same rows as 36-byte fragments. A bulk copy must start on a 16-byte
+// boundary and move a multiple of 16 bytes: each row's copy starts at the
+// boundary at or below its first node and is rounded up; a row whose
+// rounded range would leave the field's buffer is filled with plain loads.
+// ---------------------------------------------------------------------
+constexpr int kRunBricks = 8;
+constexpr int kRunNodes = kRunBricks * kBrickCells + 1;   // 65
+constexpr int kRowSlot = 72;                              // floats per staged row (288 B)
+constexpr int kRows = kBrickNodes * kBrickNodes;          // 81
+constexpr long long kStageSpin = 1ll << 22;               // bounded mbarrier wait
+
+__device__ int g_stage_timeout;  // set when a staged copy did not complete
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(const uint64_t *bar, unsigned phase)
+{
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for phase 0 of the barrier, at most kStageSpin polls.
+__device__ __forceinline__ bool mbar_wait_bounded(const uint64_t *bar)
+{
+  for (long long i = 0; i < kStageSpin; ++i) {
+    if (mbar_try_wait(bar, 0)) return true;
+    if (i > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(256)
+brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny, int nz, int nbx,
+                    int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range)
+{
+  __shared__ __align__(16) float rows[kRows * kRowSlot];
+  __shared__ int lead[kRows];
+  __shared__ int plain[kRows];
+  __shared__ __align__(8) uint64_t bar;
+  const int run = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
+  const int x0 = run * kRunBricks * kBrickCells;
+  const int count = min(kRunNodes, nx - x0);
+  const uintptr_t base = reinterpret_cast<uintptr_t>(src);
+  const uintptr_t end = base + (uintptr_t)n_src * sizeof(float);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // 16-byte-aligned copy range of row r: start a, size sz (bytes)
+  auto row_range = [&](int r, uintptr_t &a, unsigned &sz) {
+    const int y = min(by * kBrickCells + r % kBrickNodes, ny - 1);
+    const int z = min(bz * kBrickCells + r / kBrickNodes, nz - 1);
+    const uintptr_t first = base + ((uintptr_t)(((int64_t)z * ny + y) * nx + x0)) * sizeof(float);
+    a = first & ~(uintptr_t)15;
+    sz = (unsigned)(((first - a) + (uintptr_t)count * sizeof(float) + 15) & ~(uintptr_t)15);
+    return (int)((first - a) / sizeof(float));
+  };
+  // thread r plans row r: announces its bytes on the barrier and issues its
+  // bulk copy (or marks the row for plain loads); thread 0 arrives once all
+  // rows are announced, so the phase cannot complete early
+  if (threadIdx.x < kRows) {
+    const int r = threadIdx.x;
+    uintptr_t a;
+    unsigned sz;
+    lead[r] = row_range(r, a, sz);
+    plain[r] = (a < base || a + sz > end) ? 1 : 0;
+    if (!plain[r]) {
+      asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)),
+                   "r"(sz)
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_u32(rows + r * kRowSlot)),
+          "l"(a), "r"(sz), "r"(smem_u32(&bar))
+          : "memory");
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  __syncthreads();
+  bool ok = mbar_wait_bounded(&bar);
+  // rows that could not be copied in bulk: plain loads
+  for (int r = 0; r < kRows; ++r) {
+    if (!plain[r]) continue;
+    const int y = min(by * kBrickCells + r % kBrickNodes, ny - 1);
+    const int z = min(bz * kBrickCells + r / kBrickNodes, nz - 1);
+    const float *row = src + ((int64_t)z * ny + y) * nx + x0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) rows[r * kRowSlot + lead[r] + i] = row[i];
+  }
+  if (!ok) {
+    atomicOr(&g_stage_timeout, 1);
+    // the copies may still land in shared memory: wait for them once more
+    mbar_wait_bounded(&bar);
+  }
+  __syncthreads();
+  // warp w writes brick run * 8 + w
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bx = run * kRunBricks + w;
+  if (bx >= nbx) return;
+  const int64_t b = ((int64_t)bz * nby + by) * nbx + bx;
+  float *dst = bricks + b * kBrickFloats;
+  float vmin = FLT_MAX, vmax = -FLT_MAX;
+  int bad = !ok;
+  for (int l = lane; l < kBrickFloats; l += 32) {
+    float v = 0.f;
+    if (l < kBrickNodes * kBrickNodes * kBrickNodes) {
+      const int lx = l % kBrickNodes, rr = l / kBrickNodes;
+      const int x = min(bx * kBrickCells + lx, nx - 1) - x0;
+      v = rows[rr * kRowSlot + lead[rr] + x];
+      bad |= !isfinite(v);
+      vmin = fminf(vmin, v);
+      vmax = fmaxf(vmax, v);
+    }
+    dst[l] = v;
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  for (int o = 16; o > 0; o >>= 1) {
+    vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  }
+  if (lane == 0) brick_range[b] = bad ? make_float2(NAN, NAN) : make_float2(vmin, vmax);
+}
+
+}  // namespace
+
+// True (and the flag cleared) when a staged brick copy gave up waiting since
+// the last call; reads a device flag, so call it after synchronising.
+bool ingest_timed_out()
+{
+  int flag = 0;
+  if (cudaMemcpyFromSymbol(&flag, g_stage_timeout, sizeof(int)) != cudaSuccess) return false;
+  if (flag) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_stage_timeout, &zero, sizeof(int));
+  }
+  return flag != 0;
+}
+
+namespace {
+
+// Brick a field in device memory: the staged kernel for contiguous float32,
+// the per-brick gather otherwise.
+cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int dims[3],
+                          float *d_bricks, const int nbrick[3], float2 *d_brick_range,
+                          cudaStream_t stream)
+{
+  const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
+  if (dtype == GVR_DTYPE_FLOAT32 && stride == 1) {
+    const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
+    dim3 grid((unsigned)((nbrick[0] + kRunBricks - 1) / kRunBricks), (unsigned)nbrick[1],
+              (unsigned)nbrick[2]);
+    brick_staged_kernel<<<grid, 256, 0, stream>>>((const float *)dsrc, n, dims[0], dims[1], dims[2],
+                                                  nbrick[0], nbrick[1], d_bricks, d_brick_range);
+  } else {
+    brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1], dims[2],
+                                                   nbrick[0], nbrick[1], d_bricks, d_brick_range);
+  }
+  count_launch();
+  return cudaGetLastError();
 }
 
 // Strided float32/float64 -> contiguous float32 with per-CTA min/max.
@@ -167,11 +347,7 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
   cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, stg, stream);
   if (e != cudaSuccess) return e;
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
-  brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1],
-                                                 dims[2], nbrick[0], nbrick[1], d_bricks,
-                                                 d_brick_range);
-  count_launch();
-  e = cudaGetLastError();
+  e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, stream);
   if (e != cudaSuccess) return e;
   std::vector<float2> h((size_t)nb);
   e = cudaMemcpyAsync(h.data(), d_brick_range, sizeof(float2) * nb,
@@ -235,9 +411,8 @@ cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, con
                                 float2 *d_range, cudaStream_t stream)
 {
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
-  brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1], dims[2],
-                                                 nbrick[0], nbrick[1], d_bricks, d_brick_range);
-  count_launch();
+  cudaError_t e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, stream);
+  if (e != cudaSuccess) return e;
   range_of_bricks_kernel<<<1, 1024, 0, stream>>>(d_brick_range, nb, d_range);
   count_launch();
   return cudaGetLastError();

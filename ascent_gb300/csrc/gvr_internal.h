@@ -200,6 +200,9 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
                                Staging &stg, cudaStream_t stream);
+// True (flag cleared) when a staged field copy gave up waiting since the
+// last call; reads a device flag, so call it after synchronising.
+bool ingest_timed_out();
 // Brick a vertex field that is already in device memory and reduce its
 // range to *d_range on the device (no host synchronisation).
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
