@@ -1,7 +1,7 @@
 /*
  * gvr_oracle.c — CPU restatement of Ascent's volume-plot path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker that the CUDA product
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle that the CUDA product
  * is compared against; it is never linked into, loaded by, or called from
  * the product library. Only tests/, __graft_entry__.smoke() and bench.py's
  * CPU-baseline arm load it.

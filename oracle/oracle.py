@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (``oracle/gvr_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: loaded by tests/, by ``__graft_entry__.smoke()``
-as the checker, and by bench.py's CPU-baseline arm. The product library
+to compare against, and by bench.py's CPU-baseline arm. The product library
 never imports this module.
 
 Two builds of one C source:

@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in this directory from the reference tree.
 
 Run in a checkout where the Ascent sources are readable (default path
-/root/reference, override with GVR_REFERENCE_ROOT). The GPU machine never
-runs this script; tests read only the committed .npz files.
+/root/reference, override with GVR_REFERENCE_ROOT). Tests read only the
+committed .npz files.
 
 apcomp_volume_partial.npz
     The reference's baseline image of its partial-compositing test
