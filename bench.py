@@ -550,6 +550,23 @@ def run_reference(args):
     return 0
 
 
+def max_over_ranks(x: float, dist=None, device=None) -> float:
+    """Largest x over the ranks of the process group (x itself on one rank):
+    the job's time is its slowest rank's."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, units_per_step: float, steps: int, seconds: float) -> float:
+    """Whole-job rate (G units/s) of `world` replicas each doing
+    units_per_step per step, the job taking `seconds` for `steps` steps."""
+    return world * units_per_step * steps / seconds / 1e9
+
+
 def run_ours(args):
     import torch
     from ascent_gb300 import _native as N
@@ -608,10 +625,7 @@ def run_ours(args):
         dist.barrier()
     per = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = starts[0].elapsed_time(ends[-1])
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, f"cuda:{dev}")
 
     # end to end: host fields -> C ABI (upload + re-brick) -> render -> host image
     host_fields = [torch.from_numpy(d.field).pin_memory() for d in wl.domains]
@@ -639,10 +653,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{dev}")
 
     if rank != 0:
         return 0
@@ -651,8 +662,8 @@ def run_ours(args):
     alg_bytes = n_samples * BYTES_PER_SAMPLE + pixels * BYTES_PER_PIXEL
     achieved = alg_bytes / avg_launch_s / 1e9
     traffic, traffic_wl = ncu_traffic(n_samples, pixels)
-    value = world * n_samples * args.steps / (total_ms / 1e3) / 1e9
-    e2e_value = world * n_samples * e2e_steps / e2e_s / 1e9
+    value = replica_rate(world, n_samples, args.steps, total_ms / 1e3)
+    e2e_value = replica_rate(world, n_samples, e2e_steps, e2e_s)
     field_bytes = sum(d.field.nbytes for d in wl.domains)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
