@@ -395,7 +395,7 @@ int gvr_scene_destroy(gvr_scene *s)
   if (s->batch_exec) cudaGraphExecDestroy(s->batch_exec);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < gvr_scene::kStageMax; ++b) {
     cudaFree(s->stage[b]);
     if (s->copied[b]) cudaEventDestroy(s->copied[b]);
     if (s->consumed[b]) cudaEventDestroy(s->consumed[b]);
@@ -590,37 +590,50 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
   }
   if (location == GVR_MEM_HOST) {
     size_t need = 0;
+    int jobs = 0;
     for (int k = 0; k < n; ++k)
-      if (piped(s->domains[domain_ids[k]])) need = std::max(need, src_bytes(s->domains[domain_ids[k]]));
+      if (piped(s->domains[domain_ids[k]])) {
+        need = std::max(need, src_bytes(s->domains[domain_ids[k]]));
+        ++jobs;
+      }
     if (!s->copy_stream) {
       if ((e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
         return cuda_error(e, "copy stream");
-      for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+      for (int b = 0; b < gvr_scene::kStageMax && e == cudaSuccess; ++b) {
         e = cudaEventCreateWithFlags(&s->copied[b], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->consumed[b], cudaEventDisableTiming);
       }
       if (e != cudaSuccess) return cuda_error(e, "copy events");
     }
-    if (need > s->stage_bytes) {
+    // one buffer per field up to kStageMax within ~1 GB (at least two): a
+    // copy then never waits for the bricking of an earlier field, which
+    // may be held back by other work on the GPU
+    const int want = (int)std::min<int64_t>(
+        std::min(gvr_scene::kStageMax, std::max(jobs, 1)),
+        std::max<int64_t>(2, ((int64_t)1 << 30) / (int64_t)std::max<size_t>(need, 1)));
+    if (jobs > 0 && (need > s->stage_bytes || want > s->stage_count)) {
       // the old buffers may still be read by bricking from an earlier call
       if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_error(e, "staging");
-      for (int b = 0; b < 2; ++b) {
+      for (int b = 0; b < gvr_scene::kStageMax; ++b) {
         cudaFree(s->stage[b]);
         s->stage[b] = nullptr;
       }
+      const size_t bytes = std::max(need, s->stage_bytes);
       s->stage_bytes = 0;
-      for (int b = 0; b < 2; ++b)
-        if ((e = cudaMalloc(&s->stage[b], need)) != cudaSuccess) return cuda_error(e, "staging");
-      s->stage_bytes = need;
+      s->stage_count = 0;
+      for (int b = 0; b < want; ++b)
+        if ((e = cudaMalloc(&s->stage[b], bytes)) != cudaSuccess) return cuda_error(e, "staging");
+      s->stage_bytes = bytes;
+      s->stage_count = want;
     }
   }
-  // copies of field j + 1 overlap the bricking of field j
+  // copies run ahead of the bricking by up to stage_count fields
   int j = 0;
   for (int k = 0; k < n; ++k) {
     Domain &d = s->domains[domain_ids[k]];
     if (!piped(d)) continue;
     const void *dsrc = fields[k];
-    const int b = j & 1;
+    const int b = s->stage_count > 0 ? j % s->stage_count : 0;
     if (location == GVR_MEM_HOST) {
       e = cudaStreamWaitEvent(s->copy_stream, s->consumed[b], 0);
       if (e == cudaSuccess)

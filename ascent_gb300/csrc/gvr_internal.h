@@ -167,13 +167,16 @@ struct gvr_scene {
   float *d_batch_depth = nullptr;
   int64_t batch_pixels = 0;
   cudaStream_t own_stream = nullptr;
-  // batched field uploads: two staging buffers filled on a copy stream
-  // while the previous field is bricked, per-domain ranges on the device
-  void *stage[2] = {nullptr, nullptr};
+  // batched field uploads: staging buffers (up to one per domain, at most
+  // kStageMax, within ~1 GB) filled on a copy stream while earlier fields
+  // are bricked, per-domain ranges on the device
+  static constexpr int kStageMax = 8;
+  void *stage[kStageMax] = {};
+  int stage_count = 0;
   size_t stage_bytes = 0;
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t copied[2] = {nullptr, nullptr};
-  cudaEvent_t consumed[2] = {nullptr, nullptr};
+  cudaEvent_t copied[kStageMax] = {};
+  cudaEvent_t consumed[kStageMax] = {};
   float2 *d_ranges = nullptr;
   int ranges_cap = 0;
   cudaGraphExec_t batch_exec = nullptr;

@@ -249,10 +249,11 @@ GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *
  * gvr_scene_update_field would, same dtype/stride/location for all) — the
  * per-domain AddField loop of the Blueprint adapter when a simulation
  * publishes a new time step (ascent_vtkh_data_adapter.cpp:1782-2040). Host
- * fields are copied through two staging buffers on a copy stream while the
- * previous domain is bricked on `stream`; ranges are reduced on the device
- * and read back once. Host fields in pinned memory overlap best. Returns
- * after the uploads are complete. */
+ * fields are copied on a copy stream into staging buffers (up to one per
+ * domain, 8 at most, about 1 GB in all) while earlier domains are bricked
+ * on `stream`; ranges are reduced on the device and read back once. Host
+ * fields in pinned memory overlap best. Returns after the uploads are
+ * complete. */
 GVR_API int gvr_scene_update_fields(gvr_scene *scene, int n, const int *domain_ids,
                                     const void *const *fields, int dtype, int64_t stride,
                                     int location, void *stream);
