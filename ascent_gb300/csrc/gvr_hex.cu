@@ -303,6 +303,40 @@ __global__ void node_range_kernel(const float4 *__restrict__ nodes, int64_t n, f
   }
 }
 
+// Monomial coefficients of every cell's trilinear map (position and vertex
+// field), 8 float4 per cell, from its corner nodes (see hex_load).
+__global__ void coef_kernel(const float4 *__restrict__ nodes, const int4 *__restrict__ conn,
+                            int64_t n_cells, float4 *__restrict__ coef)
+{
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n_cells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int4 a = conn[2 * c], b = conn[2 * c + 1];
+    const int ids[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float4 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = nodes[ids[i]];
+    auto comb = [&](float s0, float s1, float s2, float s3, float s4, float s5, float s6, float s7,
+                    float (float4::*m)) {
+      return s0 * v[0].*m + s1 * v[1].*m + s2 * v[2].*m + s3 * v[3].*m + s4 * v[4].*m +
+             s5 * v[5].*m + s6 * v[6].*m + s7 * v[7].*m;
+    };
+    float4 *o = coef + 8 * c;
+    // c0 = v0, c1 = v1 - v0, c2 = v3 - v0, c3 = v4 - v0, c4 = v2 - v1 - v3 + v0,
+    // c5 = v5 - v1 - v4 + v0, c6 = v7 - v3 - v4 + v0,
+    // c7 = v6 - v2 - v5 - v7 + v1 + v3 + v4 - v0
+    const float w[8][8] = {{1, 0, 0, 0, 0, 0, 0, 0},   {-1, 1, 0, 0, 0, 0, 0, 0},
+                           {-1, 0, 0, 1, 0, 0, 0, 0},  {-1, 0, 0, 0, 1, 0, 0, 0},
+                           {1, -1, 1, -1, 0, 0, 0, 0}, {1, -1, 0, 0, -1, 1, 0, 0},
+                           {1, 0, 0, -1, -1, 0, 0, 1}, {-1, 1, -1, 1, 1, -1, 1, -1}};
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      o[k] = make_float4(comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::x),
+                         comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::y),
+                         comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::z),
+                         comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::w));
+  }
+}
+
 // Faces of a VTK hexahedron as local node ids, numbered like
 // hex_exit_face: r = 0, r = 1, s = 0, s = 1, t = 0, t = 1.
 __constant__ int kHexFace[6][4] = {{0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4},
@@ -417,6 +451,8 @@ void free_hex(Domain &d)
   cudaFree(d.d_inner_box);
   cudaFree(d.d_nbr);
   d.d_nbr = nullptr;
+  cudaFree(d.d_coef);
+  d.d_coef = nullptr;
   d.d_nodes = nullptr;
   d.d_conn = nullptr;
   d.d_bvh = nullptr;
@@ -487,6 +523,9 @@ int hex_update_field(Domain &d, const void *field, int dtype, int64_t stride, in
   cudaFree(flag);
   if (e != cudaSuccess) return cuda_error(e, "hex field update");
   if (bad) return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
+  coef_kernel<<<grid_for(d.n_cells), 256>>>(d.d_nodes, d.d_conn, d.n_cells, d.d_coef);
+  count_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "hex coefficients");
   return node_range(d);
 }
 
@@ -593,6 +632,9 @@ static int build_hex(Domain &d, const void *x, const void *y, const void *z, int
     HEX_TRY(cudaMemcpy(flags, d_flag, sizeof(flags), cudaMemcpyDeviceToHost), "read flags");
     if (flags[0]) { rc = set_error(GVR_ERR_INVALID_ARGUMENT, "hex coordinates or field are not finite"); goto done; }
     if (flags[1]) { rc = set_error(GVR_ERR_INVALID_ARGUMENT, "hex connectivity refers to a missing node"); goto done; }
+    HEX_TRY(dev_alloc(&d.d_coef, 8 * nc), "alloc coefficients");
+    coef_kernel<<<grid_for(nc), 256>>>(d.d_nodes, d.d_conn, nc, d.d_coef);
+    count_launch();
 
     // cell boxes + scene box
     const int gb = grid_for(nc);
@@ -669,6 +711,7 @@ done:
   d.bvh_build_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (rc == GVR_OK) rc = build_neighbours(d);
   d.dev.hex_nbr = d.d_nbr;
+  d.dev.hex_coef = d.d_coef;
   d.dev.hex_nodes = d.d_nodes;
   d.dev.hex_conn = d.d_conn;
   d.dev.hex_bvh = d.d_bvh;

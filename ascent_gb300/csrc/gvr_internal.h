@@ -43,6 +43,7 @@ struct DomainDev {
   // hexahedral domains
   const float4 *hex_nodes;    // x, y, z, vertex field value
   const int4 *hex_conn;       // 8 node ids per cell (VTK hex order), 2 int4
+  const float4 *hex_coef;     // 8 per cell: monomial coefficients of the trilinear map (xyz, field)
   const float4 *hex_bvh;      // 4 float4 per inner node (see gvr_hex.cu)
   const int *hex_ids;         // cell id of each sorted leaf
   const int *hex_nbr;         // 6 face neighbours per cell (r=0,r=1,s=0,s=1,t=0,t=1), -1 none
@@ -122,6 +123,7 @@ struct Domain {
   int64_t n_cells = 0;
   float4 *d_nodes = nullptr;
   int4 *d_conn = nullptr;
+  float4 *d_coef = nullptr;         // 8 per cell (see hex_coef)
   float4 *d_bvh = nullptr;
   uint32_t *d_codes = nullptr;      // sorted Morton codes
   uint32_t *d_ids = nullptr;        // sorted leaf -> cell id

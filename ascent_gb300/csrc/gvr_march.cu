@@ -332,11 +332,7 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
     if (dm.assoc == GVR_ASSOC_ELEMENT) {
       val = __ldg(dm.cells + cur);
     } else {
-      float n[8];
-      hex_weights(__saturatef(rst[0]), __saturatef(rst[1]), __saturatef(rst[2]), n);
-      val = 0.f;
-#pragma unroll
-      for (int i = 0; i < 8; ++i) val = fmaf(n[i], v[i].w, val);
+      val = hex_value(v, __saturatef(rst[0]), __saturatef(rst[1]), __saturatef(rst[2]));
     }
     const float s = __saturatef((val - mp.scalar_min) * mp.inv_range);
     const float4 col = lut_fetch(lut, mp.lut_size, mp.lut_filter, s);
