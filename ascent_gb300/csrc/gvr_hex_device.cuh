@@ -36,7 +36,7 @@ constexpr float kHexNewtonTol = 2e-3f;     // |step|_inf in reference space
 constexpr float kHexInsideTol = 2e-4f;     // r, s, t in [-tol, 1 + tol]
 constexpr int kHexStack = 64;
 constexpr int kHexHops = 4;                // face-neighbour steps before the LBVH walk
-constexpr float kHexPredictMargin = 0.05f; // guess this far outside: step before solving
+constexpr float kHexPredictMargin = 0.02f; // guess this far outside: step before solving
 
 // A cell's trilinear map x(r,s,t) = sum_k c_k m_k(r,s,t) over the monomials
 // m = (1, r, s, t, rs, rt, st, rst); c_k.xyz are position coefficients and
