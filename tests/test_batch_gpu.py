@@ -94,3 +94,33 @@ def test_batch_host_outputs_many_domains_and_uneven_views():
             g, gd = sc.render(cams[v], p)
             np.testing.assert_array_equal(rgba[v], g)
             np.testing.assert_array_equal(depth[v], gd)
+
+
+def test_batch_with_hex_and_uniform_domains():
+    """A scene of a uniform domain beside a hexahedral one, batched over four
+    views: each view equals the single-view render and the oracle."""
+    hw = W.hex_mesh(n_cells=10, seed=6, width=72, height=64)
+    h = hw.domains[0]
+    # a uniform block next to the hex mesh (which spans the unit cube)
+    n = 12
+    rng = np.random.default_rng(3)
+    field = rng.uniform(0.2, 1.0, (n + 1, n + 1, n + 1)).astype(np.float32)
+    origin, spacing = (1.0, 0.0, 0.0), (1.0 / n,) * 3
+    bounds = np.array([0, 2, 0, 1, 0, 1.0])
+    cams = S.cinema_cameras(bounds, W.cinema_angles(2, 2))
+    p = V.workload_params(hw)
+    p.scalar_min, p.scalar_max = 0.0, 1.0
+    with S.Scene(0) as sc:
+        sc.add_hex(h.x, h.y, h.z, h.conn, h.field)
+        sc.add_uniform(field, origin, spacing)
+        rgba, depth = sc.render_batch(cams, p)
+        for v, cam in enumerate(cams):
+            g, gd = sc.render(cam, p)
+            np.testing.assert_array_equal(rgba[v], g)
+            np.testing.assert_array_equal(depth[v], gd)
+    osc = O.OracleScene(64)
+    osc.add_hex(h.x, h.y, h.z, h.conn, h.field)
+    osc.add_uniform(field.shape[::-1], origin, spacing, field)
+    for v, cam in enumerate(cams):
+        assert_parity(rgba[v], osc.render(cam, p)[0])
+    assert rgba[..., 3].max() > 0.1

@@ -118,3 +118,23 @@ def test_render_over_empty_canvas_is_the_plain_render_and_device_in_place():
         torch.cuda.synchronize()
         np.testing.assert_array_equal(tr.cpu().numpy(), h)
         np.testing.assert_array_equal(td.cpu().numpy(), hd)
+
+
+@pytest.mark.gpu
+def test_render_over_hex_mesh_matches_oracle():
+    from ascent_gb300 import scene as S
+    wl = W.hex_mesh(n_cells=16, seed=2, width=80, height=72)
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    rgba, depth = canvas_for(wl, cam, p, seed=4)
+    h = wl.domains[0]
+    with S.Scene(0) as sc:
+        sc.add_hex(h.x, h.y, h.z, h.conn, h.field)
+        g, gd = sc.render_over(cam, p, rgba, depth)
+    osc = O.OracleScene(64)
+    osc.add_hex(h.x, h.y, h.z, h.conn, h.field)
+    o, od, on = osc.render_over(cam, p, rgba, depth)
+    assert_parity(g, o)
+    assert np.mean(np.abs(gd - od) <= 2e-4) >= 0.999
+    _, _, full = osc.render(cam, p)
+    assert on < full
