@@ -204,7 +204,9 @@ GVR_API int gvr_scene_add_rectilinear(gvr_scene *scene, const int dims[3],
  * cells of 8 node ids each in VTK hexahedron order (int32, or int64 when
  * conn_int64), and a scalar field per node (vertex) or per cell (element).
  * All arrays are in `location` memory. The domain's LBVH (Morton codes,
- * Karras radix tree, box refit) is built on the device. Replaces the
+ * Karras radix tree, box refit), face-neighbour table and per-cell
+ * monomial coefficients of the trilinear map (which the march evaluates)
+ * are built on the device. Replaces the
  * unstructured path of the Blueprint adapter
  * (ascent_vtkh_data_adapter.cpp:1618-1780) and the ConnectivityProxy set-up
  * of VolumeRenderer's UnstructuredWrapper (VolumeRenderer.cpp:182-220). */
@@ -241,7 +243,8 @@ GVR_API int gvr_scene_hex_locate(gvr_scene *scene, int domain_id, const float *p
                                  int n, int *cells, float *rst);
 
 /* Replace the field of an existing domain (same size, type rules as the
- * add call); the bricked copy and macrocell ranges are rebuilt on device. */
+ * add call); the bricked copy and macrocell ranges (hexahedral domains: the
+ * node values and cell coefficients) are rebuilt on the device. */
 GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *field,
                            int dtype, int64_t stride, int location);
 
@@ -282,9 +285,11 @@ GVR_API int gvr_scene_range(const gvr_scene *scene, double range[2]);
 /* ------------------------------------------------------------------ */
 
 /* Render the scene's volume for one camera into rgba (4*W*H floats) and
- * depth (W*H floats), both in `out_location` memory. Every structured
- * domain is marched and the per-domain partials are composited per pixel
- * by exit distance, front to back. Replaces VolumeRenderer::DoExecute with
+ * depth (W*H floats), both in `out_location` memory. Each ray visits the
+ * domains it crosses in increasing entry distance (each from the furthest
+ * exit reached so far) and composites their partials front to back, as the
+ * reference's (pixel, depth) sort of partials orders them for disjoint
+ * domains. Replaces VolumeRenderer::DoExecute with
  * RenderOneDomainPerRank / RenderMultipleDomainsPerRank, the partial
  * extraction, PartialCompositor::composite and partials_to_canvas
  * (VolumeRenderer.cpp:141-391, 469-597; PartialCompositor.cpp:57-90,
@@ -347,9 +352,10 @@ GVR_API int gvr_diff_workspace(const int dims[3], const double spacing[3], float
  * interpolated transfer function and no partial culling, so that the image
  * is differentiable in the node field and the LUT. field (node values, x
  * fastest), lut (lut_size RGBA floats), rgba (n_views * W * H * 4) and
- * checkpoints (may be NULL for an inference-only pass) are device pointers.
- * Other fields of params used: width, height, sample_dist, scalar range,
- * lut_size. */
+ * workspace (n_views * W * H * gvr_diff_workspace floats: the transmittance
+ * checkpoints and per-sample scalars the adjoint needs; NULL for an
+ * inference-only pass) are device pointers. Other fields of params used:
+ * width, height, sample_dist, scalar range, lut_size. */
 GVR_API int gvr_diff_render_forward(const float *field, const int dims[3], const double origin[3],
                                     const double spacing[3], const gvr_camera *cameras,
                                     int n_views, const gvr_render_params *params,
@@ -360,7 +366,9 @@ GVR_API int gvr_diff_render_forward(const float *field, const int dims[3], const
  * as rgba) and the forward's workspace, ADD dL/d(field) into grad_field
  * (node layout) and dL/d(lut) into grad_lut (lut_size * 4). The
  * transmittances of each 64-sample segment are rebuilt from its checkpoint;
- * the blend is never inverted. */
+ * the blend is never inverted. Scratch (a float4 per node for the
+ * field-gradient corner quads, and LUT-gradient copies of at most 512 MB)
+ * comes from the stream-ordered allocator. */
 GVR_API int gvr_diff_render_backward(const float *field, const int dims[3],
                                      const double origin[3], const double spacing[3],
                                      const gvr_camera *cameras, int n_views,
@@ -396,9 +404,9 @@ typedef struct {
  *
  * location says where both `partials` and `out` live (GVR_MEM_HOST or
  * GVR_MEM_DEVICE); n < 2^31. Scratch comes from the stream-ordered
- * allocator (about 24 bytes per record plus 16 per pixel of the id range,
- * or 56 per record when ids are sparse); the call returns after the result
- * is complete. */
+ * allocator: 8 bytes per record plus 16 per pixel of the id range (dense
+ * ids) or 40 per record (sparse ids), and 48 per record more for host
+ * arrays. The call returns after the result is complete. */
 GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_partial *out,
                                    int64_t *n_out, int location, void *stream);
 
