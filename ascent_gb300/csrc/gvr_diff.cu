@@ -116,15 +116,29 @@ __device__ __forceinline__ int64_t diff_cell(const DiffGrid &g, const float A[3]
   return ((int64_t)c[2] * g.dims[1] + c[1]) * g.dims[0] + c[0];
 }
 
-__device__ __forceinline__ float diff_value(const float *__restrict__ f, const DiffGrid &g,
-                                            int64_t base, const float w[3])
+// The 8 corners of the cell at base: (x, y, z) bits of the index are
+// (1, 2, 4).
+__device__ __forceinline__ void diff_corners(const float *__restrict__ f, const DiffGrid &g,
+                                             int64_t base, float c[8])
 {
   const int64_t sy = g.dims[0], sz = (int64_t)g.dims[0] * g.dims[1];
   const float *p = f + base;
-  const float c00 = lerp2(__ldg(p), __ldg(p + 1), w[0]);
-  const float c10 = lerp2(__ldg(p + sy), __ldg(p + sy + 1), w[0]);
-  const float c01 = lerp2(__ldg(p + sz), __ldg(p + sz + 1), w[0]);
-  const float c11 = lerp2(__ldg(p + sz + sy), __ldg(p + sz + sy + 1), w[0]);
+  c[0] = __ldg(p);
+  c[1] = __ldg(p + 1);
+  c[2] = __ldg(p + sy);
+  c[3] = __ldg(p + sy + 1);
+  c[4] = __ldg(p + sz);
+  c[5] = __ldg(p + sz + 1);
+  c[6] = __ldg(p + sz + sy);
+  c[7] = __ldg(p + sz + sy + 1);
+}
+
+__device__ __forceinline__ float diff_interp(const float c[8], const float w[3])
+{
+  const float c00 = lerp2(c[0], c[1], w[0]);
+  const float c10 = lerp2(c[2], c[3], w[0]);
+  const float c01 = lerp2(c[4], c[5], w[0]);
+  const float c11 = lerp2(c[6], c[7], w[0]);
   return lerp2(lerp2(c00, c10, w[1]), lerp2(c01, c11, w[1]), w[2]);
 }
 
@@ -173,6 +187,9 @@ diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews 
       A[a] = (o[a] - g.origin[a]) * g.inv_spacing[a];
       B[a] = d[a] * g.inv_spacing[a];
     }
+    // corners of the last cell loaded, reused while samples stay in it
+    int64_t last = -1;
+    float cc[8];
     for (int k = 0;; ++k) {
       const float t = fmaf((float)k, p.sample_dist, t0);
       if (!(t < t1)) break;
@@ -182,7 +199,11 @@ diff_forward(const float *__restrict__ field, const DiffGrid g, const DiffViews 
       }
       float w[3];
       const int64_t base = diff_cell(g, A, B, t, w);
-      const float val = diff_value(field, g, base, w);
+      if (base != last) {
+        diff_corners(field, g, base, cc);
+        last = base;
+      }
+      const float val = diff_interp(cc, w);
       if (ws) ws[p.v_offset + (int64_t)k * p.n_rays + ray] = val;
       float s_raw, wl;
       int i0;

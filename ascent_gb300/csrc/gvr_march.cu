@@ -201,8 +201,10 @@ __device__ int march_domain(const DomainDev &dm, const Ray &r, float t0, float t
 
 // Uniform grid, vertex field, no empty bricks: the hot path. UNROLL samples
 // are located and their 8 corners loaded before any of them is blended, so
-// a warp keeps UNROLL x 8 loads in flight. Blending stays sequential and
-// stops exactly where the one-sample loop stops.
+// a warp keeps UNROLL x 8 loads in flight. A sample in the cell of the one
+// before it reuses that cell's corners from registers (the same values, so
+// the result does not change). Blending stays sequential and stops exactly
+// where the one-sample loop stops.
 template <int UNROLL>
 __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, float t0,
                                              float t1, const MarchParams &mp,
@@ -221,6 +223,10 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
   const float *__restrict__ bricks = dm.bricks;
   const float nm1 = (float)(mp.lut_size - 1);
   int count = 0;
+  // corners of the last cell loaded (at half-cell spacing about half of the
+  // samples fall in the cell of the sample before)
+  int last_off = -1;
+  float lc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int k = 0;; k += UNROLL) {
     float v[UNROLL];
     bool ok[UNROLL];
@@ -240,17 +246,22 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
         off += a == 0 ? hi * kBrickFloats + lo
                       : (a == 1 ? hi * sy + lo * kBrickNodes : hi * sz + lo * kBrickNodes * kBrickNodes);
       }
-      const float *p = bricks + off;
-      const float v000 = __ldg(p), v100 = __ldg(p + 1);
-      const float v010 = __ldg(p + kBrickNodes), v110 = __ldg(p + kBrickNodes + 1);
-      const float v001 = __ldg(p + kBrickNodes * kBrickNodes);
-      const float v101 = __ldg(p + kBrickNodes * kBrickNodes + 1);
-      const float v011 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
-      const float v111 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
-      const float c00 = lerpf(v000, v100, w[0]);
-      const float c10 = lerpf(v010, v110, w[0]);
-      const float c01 = lerpf(v001, v101, w[0]);
-      const float c11 = lerpf(v011, v111, w[0]);
+      if (off != last_off) {
+        const float *p = bricks + off;
+        lc[0] = __ldg(p);
+        lc[1] = __ldg(p + 1);
+        lc[2] = __ldg(p + kBrickNodes);
+        lc[3] = __ldg(p + kBrickNodes + 1);
+        lc[4] = __ldg(p + kBrickNodes * kBrickNodes);
+        lc[5] = __ldg(p + kBrickNodes * kBrickNodes + 1);
+        lc[6] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
+        lc[7] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+        last_off = off;
+      }
+      const float c00 = lerpf(lc[0], lc[1], w[0]);
+      const float c10 = lerpf(lc[2], lc[3], w[0]);
+      const float c01 = lerpf(lc[4], lc[5], w[0]);
+      const float c11 = lerpf(lc[6], lc[7], w[0]);
       v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
     }
 #pragma unroll
