@@ -122,9 +122,10 @@ def test_odd_image_sizes_and_tiny_lut():
         assert_parity(g, o)
 
 
-def test_empty_space_skipping_is_exact():
+@pytest.mark.parametrize("parts", [(1, 1, 1), (2, 1, 2)])
+def test_empty_space_skipping_is_exact(parts):
     """Bricks whose range maps to zero opacity are skipped; samples still count."""
-    wl = W.plain_small(n=72, width=128, height=128)
+    wl = W.plain_small(n=72, width=128, height=128, parts=parts)
     vr = V.workload_renderer(wl)
     lut = vr.lut(True)
     lut[: 600, 3] = 0.0  # transparent below s = 0.586
