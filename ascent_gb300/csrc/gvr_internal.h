@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -23,6 +24,7 @@ static_assert(kBrickNodes * kBrickNodes * kBrickNodes <= kBrickFloats, "brick");
 
 constexpr int kMaxDomains = 64;     // domains a single render can composite
 constexpr int kMaxLut = 4096;
+constexpr int kMarchTile = 16;      // march kernel: one CTA per 16x16-pixel tile
 
 // Device view of one structured domain.
 struct DomainDev {
@@ -184,6 +186,9 @@ struct gvr_scene {
   cudaGraphExec_t batch_exec = nullptr;
   std::vector<unsigned char> batch_key;
   int batch_graph_builds = 0;
+  // launch order of the march kernel's tiles per tile grid (linear tile
+  // indices, nearest the image centre first); written once, then read only
+  std::map<std::pair<int, int>, int *> tile_orders;
 };
 
 namespace gvr {
@@ -235,12 +240,14 @@ cudaError_t radix_sort_pairs(K *keys, uint32_t *vals, K *keys_tmp, uint32_t *val
 void free_hex(Domain &d);
 int hex_update_field(Domain &d, const void *field, int dtype, int64_t stride, int location);
 
-// march kernel (gvr_march.cu)
+// march kernel (gvr_march.cu); CTA i renders tile d_order[i] (a linear
+// tile index, row-major over the kMarchTile grid), or tile i when d_order is
+// NULL
 cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          const MarchParams &mp, const float4 *d_lut,
                          float4 *d_rgba, float *d_depth,
                          unsigned long long *d_samples, const Tuning &tuning,
-                         bool has_hex, cudaStream_t stream);
+                         bool has_hex, const int *d_order, cudaStream_t stream);
 cudaError_t batch_grid(const MarchParams &mp, int n_views, const Tuning &tuning, bool has_hex,
                        int *grid);
 cudaError_t launch_batch(const DomainDev *d_domains, const ViewDev *d_views, const int4 *d_rects,

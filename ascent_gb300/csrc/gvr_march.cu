@@ -26,7 +26,7 @@
 namespace gvr {
 namespace {
 
-constexpr int kTile = 16;     // CTA tile edge in pixels
+constexpr int kTile = kMarchTile;  // CTA tile edge in pixels
 constexpr int kThreads = 256; // 8 warps, each a 32-ray packet
 
 struct Ray {
@@ -285,6 +285,117 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
   }
 }
 
+// Uniform grid, vertex field, with empty bricks: the march walks the ray
+// brick by brick. Entering a brick it computes the last sample before the
+// brick's exit (a whole step inside it); an empty brick's samples up to
+// there are counted and jumped over (they would blend with zero opacity),
+// and a non-empty brick's samples up to its exit run through the same
+// unrolled, corner-reusing loop as march_uniform. Compared with a test per
+// sample, the emptiness test and the exit distance are paid once per brick.
+template <int UNROLL>
+__device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, float t0,
+                                         float t1, const MarchParams &mp,
+                                         const float4 *lut, float thr, float4 &acc)
+{
+  const float dt = mp.sample_dist;
+  float A[3], B[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    A[a] = (r.o[a] - dm.origin[a]) * dm.inv_spacing[a];
+    B[a] = r.d[a] * dm.inv_spacing[a];
+  }
+  const int cmax[3] = {dm.dims[0] - 2, dm.dims[1] - 2, dm.dims[2] - 2};
+  const int sy = dm.nbrick[0] * kBrickFloats;
+  const int sz = dm.nbrick[1] * sy;
+  const float *__restrict__ bricks = dm.bricks;
+  const float nm1 = (float)(mp.lut_size - 1);
+  int count = 0;
+  int last_off = -1;
+  float lc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  int k = 0;
+  for (;;) {
+    const float t = fmaf((float)k, dt, t0);
+    if (!(t < t1)) return count;
+    int b[3];
+    float texit = t1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      b[a] = max(0, min((int)fmaf(t, B[a], A[a]), cmax[a])) >> 3;
+      if (B[a] != 0.f) {
+        const float edge = B[a] > 0.f ? (float)min((b[a] + 1) * kBrickCells, cmax[a] + 1)
+                                      : (float)(b[a] * kBrickCells);
+        texit = fminf(texit, (edge - A[a]) / B[a]);
+      }
+    }
+    // samples k .. kx - 1 lie at least one step before the exit
+    const int kx = (int)floorf((texit - t0) / dt);
+    if (dm.brick_empty[(b[2] * dm.nbrick[1] + b[1]) * dm.nbrick[0] + b[0]]) {
+      const int kn = max(kx, k + 1);  // sample k itself is in the empty brick
+      count += kn - k;
+      k = kn;
+      continue;
+    }
+    const int kend = max(kx + 1, k + 1);
+    for (; k < kend; k += UNROLL) {
+      float v[UNROLL];
+      bool ok[UNROLL];
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        float ts = fmaf((float)(k + u), dt, t0);
+        ok[u] = k + u < kend && ts < t1;
+        ts = ok[u] ? ts : t0;
+        int off = 0;
+        float w[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float g = fmaf(ts, B[a], A[a]);
+          const int c = max(0, min((int)g, cmax[a]));
+          w[a] = g - (float)c;
+          const int hi = c >> 3, lo = c & 7;
+          off += a == 0 ? hi * kBrickFloats + lo
+                        : (a == 1 ? hi * sy + lo * kBrickNodes : hi * sz + lo * kBrickNodes * kBrickNodes);
+        }
+        if (off != last_off) {
+          const float *p = bricks + off;
+          lc[0] = __ldg(p);
+          lc[1] = __ldg(p + 1);
+          lc[2] = __ldg(p + kBrickNodes);
+          lc[3] = __ldg(p + kBrickNodes + 1);
+          lc[4] = __ldg(p + kBrickNodes * kBrickNodes);
+          lc[5] = __ldg(p + kBrickNodes * kBrickNodes + 1);
+          lc[6] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
+          lc[7] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+          last_off = off;
+        }
+        const float c00 = lerpf(lc[0], lc[1], w[0]);
+        const float c10 = lerpf(lc[2], lc[3], w[0]);
+        const float c01 = lerpf(lc[4], lc[5], w[0]);
+        const float c11 = lerpf(lc[6], lc[7], w[0]);
+        v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        if (!ok[u]) break;
+        ++count;
+        const float sc = __saturatef((v[u] - mp.scalar_min) * mp.inv_range);
+        float4 col;
+        if (mp.lut_filter == GVR_LUT_LINEAR) {
+          col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, sc);
+        } else {
+          col = lut[min((int)(sc * nm1), mp.lut_size - 1)];
+        }
+        const float wa = (1.f - acc.w) * col.w;
+        acc.x = fmaf(wa, col.x, acc.x);
+        acc.y = fmaf(wa, col.y, acc.y);
+        acc.z = fmaf(wa, col.z, acc.z);
+        acc.w += wa;
+        if (acc.w >= thr) return count;
+      }
+    }
+    k = kend;
+  }
+}
+
 // Hexahedral domain: each sample is located by Newton's method in the cell
 // of the previous sample (starting from its reference coordinates moved by
 // the last Jacobian's image of the ray step); when the
@@ -457,6 +568,8 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
              !(mp.skip_empty && *dm.any_empty))
       count += march_uniform<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
+    else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX)
+      count += march_bricks<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
     else
       count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
     if (acc.w < mp.alpha_cull) continue;
@@ -521,10 +634,13 @@ __global__ void __launch_bounds__(kThreads, MINB)
 march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
              const MarchParams mp, const float4 *__restrict__ g_lut,
              float4 *__restrict__ rgba, float *__restrict__ depth,
-             unsigned long long *__restrict__ samples)
+             unsigned long long *__restrict__ samples, const int *__restrict__ order)
 {
   constexpr int PH = 32 / PW;
   constexpr int PX = kTile / PW;  // packets per tile row
+  const int tiles_x = (mp.width + kTile - 1) / kTile;
+  const int tile = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
+  const int tile_x = tile % tiles_x, tile_y = tile / tiles_x;
   extern __shared__ float4 smem[];
   float4 *lut = smem;
   DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
@@ -538,8 +654,8 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
   __syncthreads();
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int px = blockIdx.x * kTile + (warp % PX) * PW + (lane % PW);
-  const int py = blockIdx.y * kTile + (warp / PX) * PH + (lane / PW);
+  const int px = tile_x * kTile + (warp % PX) * PW + (lane % PW);
+  const int py = tile_y * kTile + (warp / PX) * PH + (lane / PW);
   const bool valid = px < mp.width && py < mp.height;
   int count = 0;
   if (valid) {
@@ -646,7 +762,7 @@ batch_kernel(const DomainDev *__restrict__ g_domains, const ViewDev *__restrict_
 namespace {
 
 using MarchFn = void (*)(const DomainDev *, const ViewDev, const MarchParams, const float4 *,
-                         float4 *, float *, unsigned long long *);
+                         float4 *, float *, unsigned long long *, const int *);
 
 template <int PW, int UNROLL, int MINB>
 MarchFn pick() { return march_kernel<PW, UNROLL, MINB>; }
@@ -676,15 +792,16 @@ MarchFn select(const Tuning &t, bool has_hex)
 cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          const MarchParams &mp, const float4 *d_lut, float4 *d_rgba,
                          float *d_depth, unsigned long long *d_samples, const Tuning &tuning,
-                         bool has_hex, cudaStream_t stream)
+                         bool has_hex, const int *d_order, cudaStream_t stream)
 {
   const size_t smem = sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains;
   MarchFn fn = select(tuning, has_hex);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(sizeof(float4) * kMaxLut + sizeof(DomainDev) * kMaxDomains));
   if (e != cudaSuccess) return e;
-  dim3 grid((mp.width + kTile - 1) / kTile, (mp.height + kTile - 1) / kTile);
-  fn<<<grid, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba, d_depth, d_samples);
+  const int64_t tiles = (int64_t)((mp.width + kTile - 1) / kTile) * ((mp.height + kTile - 1) / kTile);
+  fn<<<(unsigned)tiles, kThreads, smem, stream>>>(d_domains, view, mp, d_lut, d_rgba, d_depth,
+                                                  d_samples, d_order);
   count_launch();
   return cudaGetLastError();
 }

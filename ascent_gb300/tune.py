@@ -1,8 +1,9 @@
 """Autotuner for the march kernel's launch shape.
 
 Candidates are the shapes gvr_scene_set_tuning accepts: pixel packet width
-per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1 or 2)
-and the CTAs per SM the register budget targets (3 or 4). Every candidate
+per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1, 2,
+or 3 at 4 CTAs per SM) and the CTAs per SM the register budget targets (3
+or 4). Every candidate
 renders the caller's own view on the caller's scene; the fastest median of
 a few CUDA-event-timed launches wins. Images do not depend on the shape, so
 tuning never changes results. Winners are cached per (GPU, workload key) in
