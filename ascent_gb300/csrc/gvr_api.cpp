@@ -402,6 +402,8 @@ int gvr_scene_destroy(gvr_scene *s)
     if (s->consumed[b]) cudaEventDestroy(s->consumed[b]);
   }
   cudaFree(s->d_ranges);
+  cudaFreeHost(s->h_ranges);
+  cudaFree(s->d_flag);
   delete s;
   return GVR_OK;
 }
@@ -423,15 +425,19 @@ static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, i
     s->classify_valid = false;
     return GVR_OK;
   }
+  bool timed_out = false;
   if (d.dev.assoc == GVR_ASSOC_VERTEX) {
+    if (!s->d_flag && (e = cudaMalloc(&s->d_flag, sizeof(int))) != cudaSuccess)
+      return cuda_error(e, "cudaMalloc flag");
     e = launch_brick_field(field, dtype, stride, location == GVR_MEM_DEVICE, d.dev.dims,
-                           d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, d.stg, 0);
+                           d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, d.stg, s->d_flag,
+                           &timed_out, 0);
   } else {
     e = launch_cells_field(field, dtype, stride, location == GVR_MEM_DEVICE, (int64_t)d.n_values,
                            d.d_cells, d.range, d.stg, 0);
   }
   if (e != cudaSuccess) return cuda_error(e, "field upload");
-  if (ingest_timed_out()) return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
+  if (timed_out) return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
   if (!(std::isfinite(d.range[0]) && std::isfinite(d.range[1])))
     return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
   s->table_dirty = true;
@@ -583,12 +589,20 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
   };
   if (n > s->ranges_cap) {
     cudaFree(s->d_ranges);
+    cudaFreeHost(s->h_ranges);
     s->d_ranges = nullptr;
+    s->h_ranges = nullptr;
     s->ranges_cap = 0;
-    if ((e = cudaMalloc(&s->d_ranges, sizeof(float2) * n)) != cudaSuccess)
+    if ((e = cudaMalloc(&s->d_ranges, sizeof(float2) * (n + 1))) != cudaSuccess)
       return cuda_error(e, "cudaMalloc ranges");
+    if ((e = cudaMallocHost(&s->h_ranges, sizeof(float2) * (n + 1))) != cudaSuccess)
+      return cuda_error(e, "cudaMallocHost ranges");
     s->ranges_cap = n;
   }
+  // the timeout flag sits after the n ranges
+  int *d_timed_out = reinterpret_cast<int *>(s->d_ranges + n);
+  if ((e = cudaMemsetAsync(d_timed_out, 0, sizeof(int), st)) != cudaSuccess)
+    return cuda_error(e, "clear flag");
   if (location == GVR_MEM_HOST) {
     size_t need = 0;
     int jobs = 0;
@@ -645,7 +659,7 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
       dsrc = s->stage[b];
     }
     e = launch_brick_device(dsrc, dtype, stride, d.dev.dims, d.d_bricks, d.dev.nbrick,
-                            d.d_brick_range, s->d_ranges + k, st);
+                            d.d_brick_range, s->d_ranges + k, d_timed_out, st);
     if (e == cudaSuccess && location == GVR_MEM_HOST) e = cudaEventRecord(s->consumed[b], st);
     if (e != cudaSuccess) return cuda_error(e, "field bricking");
     ++j;
@@ -653,11 +667,13 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
   s->table_dirty = true;
   s->classify_valid = false;
   if (j > 0) {
-    std::vector<float2> r((size_t)n);
-    e = cudaMemcpyAsync(r.data(), s->d_ranges, sizeof(float2) * n, cudaMemcpyDeviceToHost, st);
+    // ranges and the timeout flag in one copy
+    const float2 *r = s->h_ranges;
+    e = cudaMemcpyAsync(s->h_ranges, s->d_ranges, sizeof(float2) * (n + 1), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "field ranges");
-    if (ingest_timed_out()) return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
+    if (reinterpret_cast<const int *>(s->h_ranges + n)[0] != 0)
+      return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
     bool bad = false;
     for (int k = 0; k < n; ++k) {
       Domain &d = s->domains[domain_ids[k]];

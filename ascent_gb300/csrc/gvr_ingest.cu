@@ -88,8 +88,6 @@ constexpr int kRowSlot = 72;                              // floats per staged r
 constexpr int kRows = kBrickNodes * kBrickNodes;          // 81
 constexpr long long kStageSpin = 1ll << 22;               // bounded mbarrier wait
 
-__device__ int g_stage_timeout;  // set when a staged copy did not complete
-
 __device__ __forceinline__ unsigned smem_u32(const void *p)
 {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -120,7 +118,8 @@ __device__ __forceinline__ bool mbar_wait_bounded(const uint64_t *bar)
 
 __global__ void __launch_bounds__(256)
 brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny, int nz, int nbx,
-                    int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range)
+                    int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range,
+                    int *__restrict__ timed_out)
 {
   __shared__ __align__(16) float rows[kRows * kRowSlot];
   __shared__ int lead[kRows];
@@ -179,7 +178,7 @@ brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny
     for (int i = threadIdx.x; i < count; i += blockDim.x) rows[r * kRowSlot + lead[r] + i] = row[i];
   }
   if (!ok) {
-    atomicOr(&g_stage_timeout, 1);
+    atomicOr(timed_out, 1);
     // the copies may still land in shared memory: wait for them once more
     mbar_wait_bounded(&bar);
   }
@@ -214,26 +213,13 @@ brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny
 
 }  // namespace
 
-// True (and the flag cleared) when a staged brick copy gave up waiting since
-// the last call; reads a device flag, so call it after synchronising.
-bool ingest_timed_out()
-{
-  int flag = 0;
-  if (cudaMemcpyFromSymbol(&flag, g_stage_timeout, sizeof(int)) != cudaSuccess) return false;
-  if (flag) {
-    const int zero = 0;
-    cudaMemcpyToSymbol(g_stage_timeout, &zero, sizeof(int));
-  }
-  return flag != 0;
-}
-
 namespace {
 
 // Brick a field in device memory: the staged kernel for contiguous float32,
 // the per-brick gather otherwise.
 cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                           float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                          cudaStream_t stream)
+                          int *d_timed_out, cudaStream_t stream)
 {
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
   if (dtype == GVR_DTYPE_FLOAT32 && stride == 1) {
@@ -241,7 +227,8 @@ cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int
     dim3 grid((unsigned)((nbrick[0] + kRunBricks - 1) / kRunBricks), (unsigned)nbrick[1],
               (unsigned)nbrick[2]);
     brick_staged_kernel<<<grid, 256, 0, stream>>>((const float *)dsrc, n, dims[0], dims[1], dims[2],
-                                                  nbrick[0], nbrick[1], d_bricks, d_brick_range);
+                                                  nbrick[0], nbrick[1], d_bricks, d_brick_range,
+                                                  d_timed_out);
   } else {
     brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1], dims[2],
                                                    nbrick[0], nbrick[1], d_bricks, d_brick_range);
@@ -340,20 +327,27 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, const int dims[3],
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
-                               Staging &stg, cudaStream_t stream)
+                               Staging &stg, int *d_timed_out, bool *timed_out,
+                               cudaStream_t stream)
 {
   const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
   const void *dsrc = nullptr;
   cudaError_t e = stage_source(src, dtype, stride, src_on_device, n, &dsrc, stg, stream);
   if (e != cudaSuccess) return e;
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
-  e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, stream);
+  e = cudaMemsetAsync(d_timed_out, 0, sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, d_timed_out, stream);
   if (e != cudaSuccess) return e;
   std::vector<float2> h((size_t)nb);
+  int flag = 0;
   e = cudaMemcpyAsync(h.data(), d_brick_range, sizeof(float2) * nb,
                       cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&flag, d_timed_out, sizeof(int), cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return e;
+  *timed_out = flag != 0;
   double lo = INFINITY, hi = -INFINITY;
   for (const float2 &r : h) {
     if (r.x != r.x || r.y != r.y) { lo = NAN; hi = NAN; break; }
@@ -408,10 +402,11 @@ __global__ void __launch_bounds__(1024) range_of_bricks_kernel(const float2 *__r
 
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                                 float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                                float2 *d_range, cudaStream_t stream)
+                                float2 *d_range, int *d_timed_out, cudaStream_t stream)
 {
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
-  cudaError_t e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, stream);
+  cudaError_t e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range,
+                                d_timed_out, stream);
   if (e != cudaSuccess) return e;
   range_of_bricks_kernel<<<1, 1024, 0, stream>>>(d_brick_range, nb, d_range);
   count_launch();

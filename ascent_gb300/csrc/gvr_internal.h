@@ -181,8 +181,12 @@ struct gvr_scene {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copied[kStageMax] = {};
   cudaEvent_t consumed[kStageMax] = {};
+  // per-domain ranges of a batched upload, then one int: the staged
+  // kernel's timeout flag; read back in one copy into pinned h_ranges
   float2 *d_ranges = nullptr;
+  float2 *h_ranges = nullptr;
   int ranges_cap = 0;
+  int *d_flag = nullptr;  // timeout flag of single-field uploads
   cudaGraphExec_t batch_exec = nullptr;
   std::vector<unsigned char> batch_key;
   int batch_graph_builds = 0;
@@ -205,19 +209,21 @@ void count_launch(int n = 1);
 uint64_t launch_count();
 
 // ingest kernels (gvr_ingest.cu)
+// Brick a vertex field and read its range back (synchronises `stream`).
+// *d_timed_out is a device int the staged kernel sets when a bulk copy did
+// not complete within its bounded wait; *timed_out receives it.
 cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, const int dims[3],
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
-                               Staging &stg, cudaStream_t stream);
-// True (flag cleared) when a staged field copy gave up waiting since the
-// last call; reads a device flag, so call it after synchronising.
-bool ingest_timed_out();
+                               Staging &stg, int *d_timed_out, bool *timed_out,
+                               cudaStream_t stream);
 // Brick a vertex field that is already in device memory and reduce its
-// range to *d_range on the device (no host synchronisation).
+// range to *d_range on the device (no host synchronisation); a staged copy
+// that gives up waiting sets *d_timed_out.
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                                 float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                                float2 *d_range, cudaStream_t stream);
+                                float2 *d_range, int *d_timed_out, cudaStream_t stream);
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, int64_t n, float *d_cells,
                                double range_out[2], Staging &stg,
