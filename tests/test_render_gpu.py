@@ -277,6 +277,35 @@ def test_every_launch_shape_gives_the_same_image():
             sc.set_tuning(packet_w=5)
 
 
+def test_image_sizes_in_turn_on_one_scene():
+    """The march launches its tiles in a per-size order (nearest the image
+    centre first); a scene rendering several sizes in turn keeps one order
+    per size. Each image equals the one a fresh scene renders, and the
+    oracle's."""
+    wl = W.plain_small(n=40, width=64, height=64, parts=(2, 1, 2))
+    cam = V.workload_camera(wl)
+    sizes = [(45, 33), (64, 64), (17, 130), (45, 33)]
+
+    def params_at(w, h):
+        wl.width, wl.height = w, h
+        return V.workload_params(wl)
+
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        got = [sc.render(cam, params_at(w, h), count_samples=True) for w, h in sizes]
+    for (w, h), (g, gd, n) in zip(sizes, got):
+        p = params_at(w, h)
+        with S.Scene(0) as fresh:
+            V.load_workload(fresh, wl)
+            f, fd, fn = fresh.render(cam, p, count_samples=True)
+        np.testing.assert_array_equal(g, f)
+        np.testing.assert_array_equal(gd, fd)
+        assert n == fn
+        o, od, on = oracle_scene(wl).render(cam, p)
+        assert_parity(g, o)
+    np.testing.assert_array_equal(got[0][0], got[3][0])
+
+
 def test_update_fields_pipelined_equals_one_by_one():
     """gvr_scene_update_fields (two staging buffers, copy stream, device
     ranges) gives the scene of eight gvr_scene_update_field calls: same
