@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -36,6 +37,47 @@ int cuda_error(cudaError_t e, const char *what)
 {
   const int code = e == cudaErrorMemoryAllocation ? GVR_ERR_OUT_OF_MEMORY : GVR_ERR_CUDA;
   return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxPoolDevices] = {};
+}  // namespace
+
+// The device's default memory pool gives its free memory back to the
+// system at every synchronisation (release threshold 0), so a call that
+// allocates tens of MB of scratch and synchronises would map fresh pages
+// every time. This library's own pool keeps what it has allocated (up to
+// its high-water mark, held until the process exits) and leaves the
+// default pool, which other libraries in the process may use, as it is.
+cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream)
+{
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return e;
+  if (device < 0 || device >= kMaxPoolDevices) return cudaMallocAsync(ptr, bytes, stream);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (!g_pools[device]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = device;
+      cudaMemPool_t created = nullptr;
+      if ((e = cudaMemPoolCreate(&created, &props)) != cudaSuccess) return e;
+      uint64_t keep = UINT64_MAX;
+      if ((e = cudaMemPoolSetAttribute(created, cudaMemPoolAttrReleaseThreshold, &keep)) !=
+          cudaSuccess) {
+        cudaMemPoolDestroy(created);
+        return e;
+      }
+      g_pools[device] = created;
+    }
+    pool = g_pools[device];
+  }
+  return cudaMallocFromPoolAsync(ptr, bytes, pool, stream);
 }
 
 namespace {

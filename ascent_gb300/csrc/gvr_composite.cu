@@ -19,8 +19,8 @@
 //   sparse ids
 //     a stable device radix sort of 64-bit keys (pixel id, order-preserving
 //     depth bits), segment flags and scans, one thread per blended pixel.
-// Scratch comes from the stream-ordered allocator (cudaMallocAsync), so
-// repeated calls reuse the pool.
+// Scratch comes from the library's stream-ordered memory pool
+// (scratch_alloc), which keeps its memory between calls.
 #include <algorithm>
 #include <cstdint>
 
@@ -356,15 +356,15 @@ extern "C" int gvr_composite_partials(const gvr_partial *partials, int64_t n, gv
     if (e != cudaSuccess) { rc = cuda_error(e, what); goto done; } \
   } while (0)
   if (location == GVR_MEM_HOST) {
-    CP_TRY(cudaMallocAsync((void **)&d_in, sizeof(Partial) * n, st), "allocate partials");
-    CP_TRY(cudaMallocAsync((void **)&d_out, sizeof(Partial) * n, st), "allocate output");
+    CP_TRY(scratch_alloc((void **)&d_in, sizeof(Partial) * n, st), "allocate partials");
+    CP_TRY(scratch_alloc((void **)&d_out, sizeof(Partial) * n, st), "allocate output");
     CP_TRY(cudaMemcpyAsync(d_in, partials, sizeof(Partial) * n, cudaMemcpyHostToDevice, st), "copy partials");
   } else {
     d_in = const_cast<Partial *>(partials);
     d_out = out;
   }
   // pixel-id range (merge computes the same, PartialCompositor.cpp:279-306)
-  CP_TRY(cudaMallocAsync((void **)&mm, 2 * sizeof(unsigned), st), "allocate range");
+  CP_TRY(scratch_alloc((void **)&mm, 2 * sizeof(unsigned), st), "allocate range");
   CP_TRY(cudaMemsetAsync(mm, 0xff, sizeof(unsigned), st), "range");
   CP_TRY(cudaMemsetAsync(mm + 1, 0, sizeof(unsigned), st), "range");
   range_kernel<<<grid_of(n), 256, 0, st>>>(d_in, n, mm);
@@ -376,7 +376,7 @@ extern "C" int gvr_composite_partials(const gvr_partial *partials, int64_t n, gv
     const int64_t r = (int64_t)hi - lo + 1;
     const bool dense = r <= 2 * n + 65536 && r < ((int64_t)1 << 31);
     const size_t bytes = dense ? dense_bytes(n, r) : sorted_bytes(n);
-    CP_TRY(cudaMallocAsync((void **)&arena.base, bytes, st), "allocate scratch");
+    CP_TRY(scratch_alloc((void **)&arena.base, bytes, st), "allocate scratch");
     totals = arena.take<uint32_t>(2);
     CP_TRY(dense ? composite_dense(d_in, n, lo, r, d_out, arena, totals, st)
                  : composite_sorted(d_in, n, d_out, arena, totals, st),

@@ -540,7 +540,7 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   cudaError_t e = cudaFuncSetAttribute(diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "shared-memory attribute");
-  // corner-quad buffer of the field gradient, from the stream-ordered pool
+  // corner-quad buffer of the field gradient, from the library's pool
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t nodes = (int64_t)g.dims[0] * g.dims[1] * g.dims[2];
   float4 *gq = nullptr;
@@ -550,9 +550,9 @@ int gvr_diff_render_backward(const float *field, const int dims[3], const double
   p.lut_copies = (int)std::max<int64_t>(
       1, std::min<int64_t>(n_cta, ((int64_t)512 << 20) / (16 * (int64_t)p.lut_size)));
   float *glc = nullptr;
-  e = cudaMallocAsync((void **)&gq, sizeof(float4) * nodes, st);
+  e = scratch_alloc((void **)&gq, sizeof(float4) * nodes, st);
   if (e != cudaSuccess) return cuda_error(e, "allocate gradient quads");
-  e = cudaMallocAsync((void **)&glc, sizeof(float) * 4 * p.lut_size * p.lut_copies, st);
+  e = scratch_alloc((void **)&glc, sizeof(float) * 4 * p.lut_size * p.lut_copies, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(glc, 0, sizeof(float) * 4 * p.lut_size * p.lut_copies, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(gq, 0, sizeof(float4) * nodes, st);
   if (e == cudaSuccess) {

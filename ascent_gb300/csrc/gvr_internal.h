@@ -204,6 +204,11 @@ int cuda_error(cudaError_t e, const char *what);
 // camera -> per-view constants (gvr_api.cpp)
 void make_view(const gvr_camera &cam, int width, int height, ViewDev *v);
 
+// stream-ordered scratch from this library's memory pool on the current
+// device (kept between calls, unlike the default pool's); free it with
+// cudaFreeAsync
+cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream);
+
 // kernels launched by this library since it was loaded
 void count_launch(int n = 1);
 uint64_t launch_count();

@@ -368,7 +368,9 @@ GVR_API int gvr_diff_render_forward(const float *field, const int dims[3], const
  * transmittances of each 64-sample segment are rebuilt from its checkpoint;
  * the blend is never inverted. Scratch (a float4 per node for the
  * field-gradient corner quads, and LUT-gradient copies of at most 512 MB)
- * comes from the stream-ordered allocator. */
+ * comes from the library's stream-ordered memory pool, which keeps the
+ * memory it has handed out (up to its high-water mark) until the process
+ * exits, so repeated calls map no new pages. */
 GVR_API int gvr_diff_render_backward(const float *field, const int dims[3],
                                      const double origin[3], const double spacing[3],
                                      const gvr_camera *cameras, int n_views,
@@ -403,10 +405,11 @@ typedef struct {
  * without contraction bit for bit.
  *
  * location says where both `partials` and `out` live (GVR_MEM_HOST or
- * GVR_MEM_DEVICE); n < 2^31. Scratch comes from the stream-ordered
- * allocator: 8 bytes per record plus 16 per pixel of the id range (dense
- * ids) or 40 per record (sparse ids), and 48 per record more for host
- * arrays. The call returns after the result is complete. */
+ * GVR_MEM_DEVICE); n < 2^31. Scratch comes from the library's
+ * stream-ordered memory pool (kept between calls, as for the adjoint): 8
+ * bytes per record plus 16 per pixel of the id range (dense ids) or 40 per
+ * record (sparse ids), and 48 per record more for host arrays. The call
+ * returns after the result is complete. */
 GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_partial *out,
                                    int64_t *n_out, int location, void *stream);
 
