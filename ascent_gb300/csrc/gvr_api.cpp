@@ -877,7 +877,9 @@ static int ensure_buffers(gvr_scene *s, int64_t pixels, int lut_size)
 static int prepare_march(gvr_scene *s, const gvr_render_params *p, cudaStream_t st, MarchParams &mp)
 {
   cudaError_t e;
-  std::memset(&mp, 0, sizeof(mp));
+  // zeroed bytewise, padding included: the batch path compares launch
+  // parameters bytewise to decide whether its captured graph still applies
+  std::memset(static_cast<void *>(&mp), 0, sizeof(mp));
   mp.width = p->width;
   mp.height = p->height;
   mp.n_domains = (int)s->domains.size();
@@ -1161,7 +1163,7 @@ int gvr_render_volume_batch(gvr_scene *s, const gvr_camera *cameras, int n_views
     int n_views, packet_w, unroll, min_blocks, tpi, has_hex;
     const void *ptrs[6];
   } key;
-  std::memset(&key, 0, sizeof(key));
+  std::memset(static_cast<void *>(&key), 0, sizeof(key));  // padding too: compared bytewise
   key.mp = mp;
   key.n_views = n_views;
   key.packet_w = s->tuning.packet_w;

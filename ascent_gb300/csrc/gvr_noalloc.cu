@@ -17,7 +17,6 @@
 // counter cleared on every call, and calls that overlap on the GPU (on
 // different streams or threads) race on it.
 #include <cfloat>
-#include <cstring>
 #include <mutex>
 
 #include "gvr_internal.h"
@@ -261,8 +260,7 @@ extern "C" int gvr_render_uniform_noalloc(const float *field, const int dims[3],
   unsigned long long *d_count = reinterpret_cast<unsigned long long *>(scratch + kScratchLutBytes);
   cudaStream_t st = (cudaStream_t)stream;
 
-  MarchParams mp;
-  std::memset(&mp, 0, sizeof(mp));
+  MarchParams mp{};
   mp.width = p->width;
   mp.height = p->height;
   mp.n_domains = 1;
