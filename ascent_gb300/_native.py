@@ -155,6 +155,7 @@ _SIGS = {
     "gvr_render_volume_over": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams),
                                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                          C.POINTER(C.c_uint64)]),
+    "gvr_canvas_to_rgba8": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
     "gvr_composite_partials": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int64),
                                          C.c_int, C.c_void_p]),
 }

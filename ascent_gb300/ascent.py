@@ -373,7 +373,7 @@ class Ascent:
         cam = S.camera_reset_to_bounds(bounds)
         if "camera" in render:
             apply_camera(cam, render["camera"])
-        rgba, depth = sc.render(cam, params)
+        rgba, depth = sc.render(cam, params, device_out=True)
         path = PNG.save_canvas(self._dir / name, rgba)
         self._info["images"].append({"image_name": str(path), "image_width": params.width,
                                      "image_height": params.height, "camera": cam.as_dict(),
@@ -385,7 +385,7 @@ class Ascent:
         cams = S.cinema_cameras(bounds, angles)
         db = render.get("db_name", name)
         base = self._dir / "cinema_databases" / db / f"{self._time():g}"
-        rgba, _ = sc.render_batch(cams, params)
+        rgba, _ = sc.render_batch(cams, params, device_out=True)
         lines = ["phi,theta,time,FILE"]
         for (phi, theta), img, cam in zip(angles, rgba, cams):
             fname = f"{_angle(phi)}_{_angle(theta)}_{name}.png"

@@ -1,10 +1,12 @@
 """PNG output of a rendered canvas, as Ascent writes it.
 
-encode_canvas follows PNGEncoder::Encode(const float*)
+The pixel conversion follows PNGEncoder::Encode(const float*)
 (src/libs/png_utils/ascent_png_encoder.cpp:77-118): rows are flipped (the
 canvas has y up, PNG rows run top down) and every channel is converted with
-a truncating cast of value * 255. The file is an 8-bit RGBA PNG written with
-zlib (the encoding itself is host-side post-processing, outside the hot path).
+a truncating cast of value * 255. A canvas that lives on the GPU is
+converted there (gvr_canvas_to_rgba8), so only its 4 bytes per pixel come
+back to the host; a host canvas is converted with numpy. The file is an
+8-bit RGBA PNG written with zlib (the deflate is host-side).
 """
 from __future__ import annotations
 
@@ -22,6 +24,26 @@ def canvas_to_rgba8(rgba: np.ndarray) -> np.ndarray:
     return x.astype(np.uint8)
 
 
+def canvas_to_rgba8_device(rgba):
+    """canvas_to_rgba8 on the GPU: a (H, W, 4) float32 CUDA tensor -> a
+    (H, W, 4) uint8 CUDA tensor, row 0 = top, stream-ordered on the tensor's
+    current stream (gvr_canvas_to_rgba8)."""
+    import ctypes as C
+
+    import torch
+
+    from . import _native as N
+    if rgba.dtype != torch.float32 or not rgba.is_cuda or rgba.dim() != 3 or rgba.shape[2] != 4:
+        raise ValueError("canvas must be a (H, W, 4) float32 CUDA tensor")
+    src = rgba.contiguous()
+    h, w, _ = src.shape
+    out = torch.empty((h, w, 4), dtype=torch.uint8, device=src.device)
+    stream = torch.cuda.current_stream(src.device).cuda_stream
+    N.call("gvr_canvas_to_rgba8", C.c_void_p(src.data_ptr()), int(w), int(h),
+           C.c_void_p(out.data_ptr()), N.MEM_DEVICE, C.c_void_p(stream))
+    return out
+
+
 def _chunk(tag: bytes, data: bytes) -> bytes:
     return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
 
@@ -33,11 +55,16 @@ def encode_rgba8(img: np.ndarray) -> bytes:
             _chunk(b"IDAT", zlib.compress(raw, 6)) + _chunk(b"IEND", b""))
 
 
-def save_canvas(path, rgba: np.ndarray) -> Path:
-    """Write a float canvas as `path` (".png" appended when missing)."""
+def save_canvas(path, rgba) -> Path:
+    """Write a float canvas — a numpy array, or a CUDA tensor converted on
+    the device — as `path` (".png" appended when missing)."""
     p = Path(path)
     if p.suffix.lower() != ".png":
         p = p.with_name(p.name + ".png")
     p.parent.mkdir(parents=True, exist_ok=True)
-    p.write_bytes(encode_rgba8(canvas_to_rgba8(rgba)))
+    if isinstance(rgba, np.ndarray):
+        img = canvas_to_rgba8(rgba)
+    else:
+        img = canvas_to_rgba8_device(rgba).cpu().numpy()
+    p.write_bytes(encode_rgba8(img))
     return p

@@ -413,6 +413,18 @@ typedef struct {
 GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_partial *out,
                                    int64_t *n_out, int location, void *stream);
 
+/* Convert a float canvas (width x height RGBA, row 0 at the bottom, the
+ * layout gvr_render_volume writes) into the 8-bit rows of its PNG: rows
+ * flipped so that row 0 is the top one, each channel
+ * (unsigned char)(value * 255) after clamping to [0, 255] — the pixel loop
+ * of PNGEncoder::Encode(const float *) (png_utils/ascent_png_encoder.cpp:
+ * 77-118), run on the device. `out` holds width * height * 4 bytes.
+ * location says where both buffers live; with GVR_MEM_HOST the call copies
+ * in and out and returns when `out` is written, with GVR_MEM_DEVICE it is
+ * stream-ordered on `stream`. */
+GVR_API int gvr_canvas_to_rgba8(const float *rgba, int width, int height, uint8_t *out,
+                                int location, void *stream);
+
 /* Render one uniform domain without allocating any device memory; no
  * counterpart in the reference. For callers that may not call cudaMalloc or
  * cudaFree — typically a simulation that gives all GPU memory to its own

@@ -126,3 +126,28 @@ def test_errors_are_caught_or_forwarded(tmp_path):
     with pytest.raises(N.GvrError):
         b.execute([{"action": "add_scenes", "scenes": {"s": {"plots": {
             "p": {"type": "volume", "field": "braid", "samples": 0}}}}}])
+
+
+@pytest.mark.parametrize("size", [(1, 1), (37, 5), (256, 130)])
+def test_device_png_conversion_equals_host(size):
+    """gvr_canvas_to_rgba8 (device) and canvas_to_rgba8 (numpy) give the same
+    bytes: flip, value * 255, clamp, truncation — also for values outside
+    [0, 1] and on the exact steps k / 255."""
+    import ctypes as C
+    import torch
+    from ascent_gb300 import _native as N
+    w, h = size
+    rng = np.random.default_rng(w * 1000 + h)
+    img = rng.uniform(-0.2, 1.2, (h, w, 4)).astype(np.float32)
+    steps = (np.arange(h * w * 4) % 256).astype(np.float32).reshape(h, w, 4) / np.float32(255.0)
+    img[::2] = steps[::2]
+    want = PNG.canvas_to_rgba8(img)
+    got = PNG.canvas_to_rgba8_device(torch.from_numpy(img).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(got, want)
+    out = np.empty((h, w, 4), np.uint8)
+    N.call("gvr_canvas_to_rgba8", C.c_void_p(img.ctypes.data), w, h, C.c_void_p(out.ctypes.data),
+           N.MEM_HOST, None)
+    np.testing.assert_array_equal(out, want)
+    with pytest.raises(N.GvrError):
+        N.call("gvr_canvas_to_rgba8", C.c_void_p(img.ctypes.data), 0, h, C.c_void_p(out.ctypes.data),
+               N.MEM_HOST, None)
