@@ -16,6 +16,10 @@
  *     default stream. Calls are stream-ordered; host outputs are complete
  *     when the call returns.
  *   - GVR_MEM_HOST / GVR_MEM_DEVICE say where a caller buffer lives.
+ *   - A gvr_scene is used by one host thread at a time. Different scenes
+ *     may be driven from different threads at once: each has its own
+ *     device state, staging buffers, copy stream and timeout flag, and the
+ *     library's shared scratch pool and launch counter are thread-safe.
  */
 #ifndef GVR_H
 #define GVR_H
