@@ -684,8 +684,12 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
       s->stage_count = want;
     }
   }
-  // copies run ahead of the bricking by up to stage_count fields
+  // copies run ahead of the bricking by up to stage_count fields; the
+  // domains' ranges are reduced in one launch after the last field
   int j = 0;
+  std::vector<const float2 *> job_ranges;
+  std::vector<int64_t> job_bricks;
+  std::vector<float2 *> job_out;
   for (int k = 0; k < n; ++k) {
     Domain &d = s->domains[domain_ids[k]];
     if (!piped(d)) continue;
@@ -701,10 +705,17 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
       dsrc = s->stage[b];
     }
     e = launch_brick_device(dsrc, dtype, stride, d.dev.dims, d.d_bricks, d.dev.nbrick,
-                            d.d_brick_range, s->d_ranges + k, d_timed_out, st);
+                            d.d_brick_range, d_timed_out, st);
     if (e == cudaSuccess && location == GVR_MEM_HOST) e = cudaEventRecord(s->consumed[b], st);
     if (e != cudaSuccess) return cuda_error(e, "field bricking");
+    job_ranges.push_back(d.d_brick_range);
+    job_bricks.push_back(d.n_bricks);
+    job_out.push_back(s->d_ranges + k);
     ++j;
+  }
+  if (j > 0) {
+    e = launch_ranges_of_bricks(j, job_ranges.data(), job_bricks.data(), job_out.data(), st);
+    if (e != cudaSuccess) return cuda_error(e, "field ranges");
   }
   s->table_dirty = true;
   s->classify_valid = false;

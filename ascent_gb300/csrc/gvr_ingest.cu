@@ -366,13 +366,22 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
 
 namespace {
 
-// One block: min and max over the per-brick ranges into *out (NaN when any
-// brick holds a non-finite value).
-__global__ void __launch_bounds__(1024) range_of_bricks_kernel(const float2 *__restrict__ r,
-                                                               int64_t nb, float2 *__restrict__ out)
+// Jobs of one range reduction launch: one block per domain.
+constexpr int kRangeJobs = 64;
+struct RangeJobs {
+  const float2 *ranges[kRangeJobs];
+  int64_t n_bricks[kRangeJobs];
+  float2 *out[kRangeJobs];
+};
+
+// Block j: min and max over domain j's per-brick ranges into *out[j] (NaN
+// when any brick holds a non-finite value).
+__global__ void __launch_bounds__(1024) range_of_bricks_kernel(const RangeJobs jobs)
 {
   __shared__ float lo_s[32], hi_s[32];
   __shared__ int bad_s;
+  const float2 *__restrict__ r = jobs.ranges[blockIdx.x];
+  const int64_t nb = jobs.n_bricks[blockIdx.x];
   if (threadIdx.x == 0) bad_s = 0;
   __syncthreads();
   float lo = INFINITY, hi = -INFINITY;
@@ -399,7 +408,7 @@ __global__ void __launch_bounds__(1024) range_of_bricks_kernel(const float2 *__r
       lo = fminf(lo, lo_s[i]);
       hi = fmaxf(hi, hi_s[i]);
     }
-    *out = bad_s ? make_float2(NAN, NAN) : make_float2(lo, hi);
+    *jobs.out[blockIdx.x] = bad_s ? make_float2(NAN, NAN) : make_float2(lo, hi);
   }
 }
 
@@ -407,15 +416,30 @@ __global__ void __launch_bounds__(1024) range_of_bricks_kernel(const float2 *__r
 
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                                 float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                                float2 *d_range, int *d_timed_out, cudaStream_t stream)
+                                int *d_timed_out, cudaStream_t stream)
 {
-  const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
-  cudaError_t e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range,
-                                d_timed_out, stream);
-  if (e != cudaSuccess) return e;
-  range_of_bricks_kernel<<<1, 1024, 0, stream>>>(d_brick_range, nb, d_range);
-  count_launch();
-  return cudaGetLastError();
+  return launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, d_timed_out,
+                       stream);
+}
+
+cudaError_t launch_ranges_of_bricks(int n, const float2 *const *brick_ranges,
+                                    const int64_t *n_bricks, float2 *const *out,
+                                    cudaStream_t stream)
+{
+  for (int j0 = 0; j0 < n; j0 += kRangeJobs) {
+    RangeJobs jobs{};
+    const int m = std::min(kRangeJobs, n - j0);
+    for (int j = 0; j < m; ++j) {
+      jobs.ranges[j] = brick_ranges[j0 + j];
+      jobs.n_bricks[j] = n_bricks[j0 + j];
+      jobs.out[j] = out[j0 + j];
+    }
+    range_of_bricks_kernel<<<m, 1024, 0, stream>>>(jobs);
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,

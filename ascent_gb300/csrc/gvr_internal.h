@@ -223,12 +223,17 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
                                float2 *d_brick_range, double range_out[2],
                                Staging &stg, int *d_timed_out, bool *timed_out,
                                cudaStream_t stream);
-// Brick a vertex field that is already in device memory and reduce its
-// range to *d_range on the device (no host synchronisation); a staged copy
-// that gives up waiting sets *d_timed_out.
+// Brick a vertex field that is already in device memory, with per-brick
+// ranges (no host synchronisation); a staged copy that gives up waiting
+// sets *d_timed_out.
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                                 float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                                float2 *d_range, int *d_timed_out, cudaStream_t stream);
+                                int *d_timed_out, cudaStream_t stream);
+// Reduce n domains' per-brick ranges to one range each (*out[j]; NaN when a
+// brick holds a non-finite value): one launch, one block per domain.
+cudaError_t launch_ranges_of_bricks(int n, const float2 *const *brick_ranges,
+                                    const int64_t *n_bricks, float2 *const *out,
+                                    cudaStream_t stream);
 cudaError_t launch_cells_field(const void *src, int dtype, int64_t stride,
                                int src_on_device, int64_t n, float *d_cells,
                                double range_out[2], Staging &stg,
