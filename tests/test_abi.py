@@ -129,3 +129,23 @@ def test_visibility_order_matches_oracle():
                                    ref.ctypes.data_as(C.POINTER(C.c_int)))
     np.testing.assert_array_equal(got, ref)
     assert sorted(got.tolist()) == list(range(37))
+
+
+def test_canvas_conversion_rejects_bad_arguments_before_any_device_work():
+    lib = N.lib()
+    img = np.zeros((2, 3, 4), np.float32)
+    out = np.zeros((2, 3, 4), np.uint8)
+    cases = [(img.ctypes.data, 0, 2, out.ctypes.data, N.MEM_HOST, "image size"),
+             (img.ctypes.data, 3, 2, None, N.MEM_HOST, "NULL"),
+             (img.ctypes.data, 3, 2, out.ctypes.data, 7, "bad location")]
+    for src, w, h, dst, loc, msg in cases:
+        rc = lib.gvr_canvas_to_rgba8(C.c_void_p(src), w, h, C.c_void_p(dst), loc, None)
+        assert rc == N.GVR_ERR_INVALID_ARGUMENT
+        assert msg in lib.gvr_last_error().decode()
+
+
+def test_device_png_conversion_wants_a_cuda_tensor():
+    torch = pytest.importorskip("torch")
+    from ascent_gb300 import png as PNG
+    with pytest.raises(ValueError):
+        PNG.canvas_to_rgba8_device(torch.zeros((2, 2, 4), dtype=torch.float32))
