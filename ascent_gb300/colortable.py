@@ -2,21 +2,36 @@
 
 parse_color_table follows Ascent's parse_color_table
 (src/libs/ascent/runtimes/flow_filters/ascent_runtime_conduit_to_vtkm_parsing.cpp:199-305):
-  - the default table is "cool to warm"; an unknown `name` falls back to it;
+  - the default table is "cool to warm"; a `name` is accepted when it equals
+    one of VTK-m's preset names ignoring case (is_valid_name / string_equal,
+    :37-57, :176-197), otherwise the plot keeps "cool to warm" and a message
+    says so (:220-234);
+  - a preset brings its colours and its opacity points (0, 1) and (1, 1);
   - when `control_points` hold any `rgb` point and no `name` was given, the
-    preset's colours are cleared so only the given points remain;
+    preset's colours are cleared so only the given points remain; its
+    opacity points stay (ClearColors touches colours only);
   - rgb colours and alpha values are clamped to [0, 1];
   - a point at an existing position replaces the earlier one;
-  - `reverse: "true"` mirrors the colour points.
-Presets: "cool to warm" is built from the diverging colour map of
-K. Moreland, "Diverging Color Maps for Scientific Visualization" (ISVC 2009):
-linear interpolation in the Msh space derived from CIELAB between the end
-points (59, 76, 192) and (180, 4, 38), through white at the centre; it is
-sampled into 33 RGB control points. "grayscale" runs black to white.
+  - `reverse: "true"` mirrors the colour points (ReverseColors).
+Presets:
+  - "Cool to Warm" is built from the diverging colour map of K. Moreland,
+    "Diverging Color Maps for Scientific Visualization" (ISVC 2009): linear
+    interpolation in the Msh space derived from CIELAB between the end points
+    (59, 76, 192) and (180, 4, 38), through white at the centre, sampled into
+    257 RGB control points;
+  - the other 17 presets are the reference's own 256-sample renderings of
+    VTK-m's tables (src/docs/sphinx/Actions/color_tables/vtkm/<name>.png,
+    decoded into data/vtkm_presets.npz by data/make_presets.py), as 256 RGB
+    control points at positions i / 255.
+A preset's opacity points (0, 1) and (1, 1) are assumed from the reference's
+documentation (a volume plot given a colour table without alpha points
+"will look exactly the same as a pseudocolor plot", Actions/Scenes.rst);
+VTK-m's preset definitions are not part of the reference tree.
 """
 from __future__ import annotations
 
 import math
+from pathlib import Path
 
 import numpy as np
 
@@ -109,21 +124,56 @@ def diverging(rgb1, rgb2, x):
     return _lab_to_rgb(_msh_to_lab(msh))
 
 
-def _cool_to_warm(n=33):
+def _cool_to_warm(n=257):
     c1 = (59 / 255, 76 / 255, 192 / 255)
     c2 = (180 / 255, 4 / 255, 38 / 255)
     xs = np.linspace(0, 1, n)
     return xs, np.array([diverging(c1, c2, float(x)) for x in xs])
 
 
-def preset(name: str):
-    """(positions, rgb) of a named preset, or None if unknown."""
-    key = name.strip().lower()
-    if key in ("cool to warm", "cool2warm", "coolwarm"):
-        return _cool_to_warm()
-    if key in ("grayscale", "grey", "gray", "greyscale"):
-        return np.array([0.0, 1.0]), np.array([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]])
+# opacity points every preset brings (position -> alpha)
+PRESET_ALPHA = {0.0: 1.0, 1.0: 1.0}
+
+_DATA = Path(__file__).resolve().parent / "data" / "vtkm_presets.npz"
+_bars: dict | None = None
+
+
+def _color_bars() -> dict:
+    global _bars
+    if _bars is None:
+        with np.load(_DATA) as d:
+            _bars = {k: d[k] for k in d.files}
+    return _bars
+
+
+def preset_names() -> list:
+    """VTK-m's preset names, as the reference accepts them."""
+    return sorted(_color_bars())
+
+
+def _string_equal(a: str, b: str) -> bool:
+    """string_equal (conduit_to_vtkm_parsing.cpp:37-57): same length, equal
+    ignoring case."""
+    return len(a) == len(b) and a.lower() == b.lower()
+
+
+def canonical_name(name: str) -> str | None:
+    """The preset name `name` denotes, or None if the reference rejects it."""
+    for k in preset_names():
+        if _string_equal(k, str(name)):
+            return k
     return None
+
+
+def preset(name: str):
+    """(positions, rgb) of a named preset, or None if the name is not one."""
+    key = canonical_name(name)
+    if key is None:
+        return None
+    if key == "Cool to Warm":
+        return _cool_to_warm()
+    bar = _color_bars()[key].astype(np.float64) / 255.0
+    return np.arange(len(bar)) / (len(bar) - 1.0), bar
 
 
 def parse_color_table(node: dict | None, warn=print) -> TransferFunction:
@@ -138,7 +188,7 @@ def parse_color_table(node: dict | None, warn=print) -> TransferFunction:
             warn(f"Invalid color table name '{node['name']}'. Defaulting to {DEFAULT_NAME}")
     pos, rgb = preset(name)
     colors = {float(p): tuple(float(c) for c in col) for p, col in zip(pos, rgb)}
-    alphas: dict = {}
+    alphas = dict(PRESET_ALPHA)
     points = node.get("control_points", [])
     if isinstance(points, dict):
         points = list(points.values())
@@ -163,10 +213,6 @@ def parse_color_table(node: dict | None, warn=print) -> TransferFunction:
         colors = {1.0 - x: c for x, c in colors.items()}
     cx = np.array(sorted(colors))
     crgb = np.array([colors[x] for x in cx]).reshape(-1, 3)
-    if alphas:
-        ax = np.array(sorted(alphas))
-        av = np.array([alphas[x] for x in ax])
-    else:
-        default = TransferFunction.default()
-        ax, av = default.alpha_pos, default.alpha
+    ax = np.array(sorted(alphas))
+    av = np.array([alphas[x] for x in ax])
     return TransferFunction(cx, crgb, ax, av)

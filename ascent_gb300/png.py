@@ -7,6 +7,10 @@ a truncating cast of value * 255. A canvas that lives on the GPU is
 converted there (gvr_canvas_to_rgba8), so only its 4 bytes per pixel come
 back to the host; a host canvas is converted with numpy. The file is an
 8-bit RGBA PNG written with zlib (the deflate is host-side).
+
+decode_png reads PNGs back to RGBA8 (the role of PNGDecoder::Decode,
+src/libs/png_utils/ascent_png_decoder.cpp), for comparing written images and
+for reading colour-bar images.
 """
 from __future__ import annotations
 
@@ -68,3 +72,76 @@ def save_canvas(path, rgba) -> Path:
         img = canvas_to_rgba8_device(rgba).cpu().numpy()
     p.write_bytes(encode_rgba8(img))
     return p
+
+
+def decode_png(data: bytes) -> np.ndarray:
+    """(H, W, 4) uint8 RGBA of a non-interlaced PNG, top row first: 8-bit
+    grey, RGB or RGBA, or palette images of 1/2/4/8-bit indices with tRNS
+    transparency (row filters 0-4)."""
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG")
+    pos, idat, hdr, plte, trns = 8, b"", None, None, b""
+    while pos < len(data):
+        ln, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        chunk = data[pos + 8:pos + 8 + ln]
+        pos += 12 + ln
+        if typ == b"IHDR":
+            hdr = struct.unpack(">IIBBBBB", chunk)
+        elif typ == b"PLTE":
+            plte = np.frombuffer(chunk, dtype=np.uint8).reshape(-1, 3)
+        elif typ == b"tRNS":
+            trns = chunk
+        elif typ == b"IDAT":
+            idat += chunk
+        elif typ == b"IEND":
+            break
+    if hdr is None:
+        raise ValueError("PNG without IHDR")
+    w, h, depth, ctype, _, _, interlace = hdr
+    if interlace != 0 or ctype not in (0, 2, 3, 6) or (depth != 8 and ctype != 3):
+        raise ValueError(f"unsupported PNG: colour type {ctype}, depth {depth}, interlace {interlace}")
+    ch = {0: 1, 6: 4, 2: 3, 3: 1}[ctype]
+    raw = zlib.decompress(idat)
+    stride = (w * ch * depth + 7) // 8
+    bpp = max(1, ch * depth // 8)
+    out = np.zeros((h, stride), dtype=np.uint8)
+    prev = np.zeros(stride, dtype=np.int32)
+    for y in range(h):
+        f = raw[y * (stride + 1)]
+        line = np.frombuffer(raw, dtype=np.uint8, count=stride, offset=y * (stride + 1) + 1).astype(np.int32)
+        if f == 0:
+            cur = line
+        elif f == 2:
+            cur = (line + prev) & 255
+        else:
+            cur = np.zeros(stride, dtype=np.int32)
+            for x in range(stride):
+                a = cur[x - bpp] if x >= bpp else 0
+                b = prev[x]
+                c = prev[x - bpp] if x >= bpp else 0
+                if f == 1:
+                    pr = a
+                elif f == 3:
+                    pr = (a + b) // 2
+                else:  # Paeth
+                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                    pr = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                cur[x] = (line[x] + pr) & 255
+        out[y] = cur
+        prev = cur
+    if ctype == 3:
+        per = 8 // depth
+        idx = np.zeros((h, stride * per), dtype=np.int32)
+        for k in range(per):
+            idx[:, k::per] = (out >> (8 - depth * (k + 1))) & ((1 << depth) - 1)
+        idx = idx[:, :w]
+        alpha = np.full(len(plte), 255, np.uint8)
+        alpha[:len(trns)] = np.frombuffer(trns, dtype=np.uint8)
+        rgba = np.concatenate([plte, alpha[:, None]], axis=1)
+        return rgba[idx]
+    img = out.reshape(h, w, ch)
+    if ch == 1:
+        img = np.repeat(img, 3, axis=2)
+    if img.shape[2] == 3:
+        img = np.concatenate([img, np.full((h, w, 1), 255, np.uint8)], axis=2)
+    return img

@@ -2,6 +2,7 @@
 
 Reference: src/libs/vtkh/rendering/VolumeRenderer.cpp
   - defaults: 100 samples, alpha points (0, 0.02) and (0, 0.5)     :395-407
+    added to the renderer's "Cool to Warm" table (Renderer.cpp:13)
   - CorrectOpacity: a' = 1 - (1 - a)^(10 / samples)                 :448-466
   - DoExecute: one structured domain -> RenderOneDomainPerRank,
     which round-trips the canvas through a uint8 vtkh::Image;
@@ -33,13 +34,19 @@ class TransferFunction:
 
     @staticmethod
     def default() -> "TransferFunction":
-        # VolumeRenderer's constructor adds alpha points (0, .02) and (0, .5);
-        # a point added at an existing position replaces it, leaving (0, .5).
-        # Colours: the diverging "cool to warm" end points.
-        return TransferFunction(np.array([0.0, 1.0]),
-                                np.array([[0.23137254902, 0.298039215686, 0.752941176471],
-                                          [0.705882352941, 0.0156862745098, 0.149019607843]]),
-                                np.array([0.0]), np.array([0.5]))
+        """The table of a volume plot without a `color_table` node: the
+        renderer's "Cool to Warm" preset (Renderer.cpp:13) with its opacity
+        points (0, 1) and (1, 1), to which VolumeRenderer's constructor adds
+        alpha points (0, .02) and then (0, .5) (VolumeRenderer.cpp:402-405); a
+        point added at an existing position replaces it, leaving (0, .5) and
+        (1, 1)."""
+        from . import colortable as CT
+        pos, rgb = CT.preset(CT.DEFAULT_NAME)
+        alphas = dict(CT.PRESET_ALPHA)
+        alphas[0.0] = 0.02
+        alphas[0.0] = 0.5
+        ax = np.array(sorted(alphas))
+        return TransferFunction(np.asarray(pos), np.asarray(rgb), ax, np.array([alphas[x] for x in ax]))
 
 
 class VolumeRenderer:

@@ -144,11 +144,66 @@ def bricked_bytes(wl) -> int:
     return total
 
 
+def workloads_module():
+    """The seeded input generator (ascent_gb300/workloads.py, numpy only),
+    loaded from its file so that the CPU arm never imports the product
+    package or maps its library."""
+    import importlib.util
+    name = "gvr_bench_workloads"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, ROOT / "ascent_gb300" / "workloads.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def setup_workload(args):
-    from ascent_gb300 import workloads as W
+    W = workloads_module()
     t = time.time()
     wl = W.plain_large(n_cells=args.cells, width=args.size, height=args.size)
     return wl, time.time() - t
+
+
+def bench_config(wl, args) -> dict:
+    """The workload description both arms print, key for key."""
+    return {"workload": wl.name, "grid_nodes": args.cells + 1, "domains": len(wl.domains),
+            "image": [wl.width, wl.height], "samples_param": wl.samples,
+            "sample_dist_cells": 0.5, "early_term": 0.99,
+            "lut": "1024-entry float LUT for both arms; the reference's multi-domain "
+                   "uint8 LUT would round opacity to 0 below s=0.98 at 1774 samples",
+            "l2": f"inputs {bricked_bytes(wl) / 2**20:.0f} MiB bricked on the GPU (L2 129 MB); "
+                  "not flushed"}
+
+
+def oracle_setup(wl, *, float_lut=False, camera=None):
+    """Camera and render parameters built by the oracle's own functions
+    (never the product library's): opacity correction, LUT sampling, sample
+    distance and camera. float_lut: the benchmark's 1024-entry float LUT on
+    the multi-domain path; camera: (phi, theta) of a Cinema view instead of
+    the workload's reset + azimuth + elevation camera."""
+    from oracle import oracle as O
+    if camera is None:
+        cam = O.workload_camera(wl)
+    else:
+        cam = O.cinema_cameras(wl.bounds, [camera])[0]
+    if float_lut:
+        params = O.workload_params(wl, lut=O.workload_lut(wl, single_domain=True), single_domain=False)
+    else:
+        params = O.workload_params(wl)
+    return cam, params
+
+
+def oracle_scene_of(wl, precision):
+    from oracle import oracle as O
+    osc = O.OracleScene(precision)
+    for d in wl.domains:
+        if hasattr(d, "conn"):
+            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
+        else:
+            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    return osc
 
 
 def bench_params(wl):
@@ -160,34 +215,51 @@ def bench_params(wl):
     return vr.params(wl.width, wl.height, wl.bounds, wl.scalar_range, single_domain=False, lut=lut), N
 
 
-def cpu_sample(wl, cam, params, seconds: float, per_step: bool = False):
-    """Time the FP32 OpenMP oracle port on central row bands until `seconds` pass."""
+def cpu_sample(wl, seconds: float, *, float_lut=False, camera=None):
+    """Time the FP32 OpenMP port of the oracle on this host's cores for about
+    `seconds`: whole frames when one frame fits in a third of that, else
+    bands of image rows (at least four rows per thread, walking outwards from
+    the centre row) so that every thread has rows to render. Camera and
+    parameters are built by the oracle (oracle_setup)."""
     from oracle import oracle as O
-    osc = O.OracleScene(32)
-    for d in wl.domains:
-        if hasattr(d, "conn"):
-            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
-        else:
-            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    cam, params = oracle_setup(wl, float_lut=float_lut, camera=camera)
+    osc = oracle_scene_of(wl, 32)
+    threads = O.num_threads(32)
     h, w = params.height, params.width
     rgba = np.zeros((h, w, 4), np.float32)
     depth = np.zeros((h, w), np.float32)
-    band = 8
-    row = h // 2 - band // 2
-    samples = rows = 0
+    # probe: a band of 4 rows per thread around the centre
+    band = min(h, 4 * threads)
+    r0 = max(0, h // 2 - band // 2)
     t0 = time.perf_counter()
-    while True:
-        r0 = row % h
-        r1 = min(r0 + band, h)
-        samples += osc.render_rows(cam, params, r0, r1, rgba, depth)
-        rows += r1 - r0
-        row = r1 if r1 < h else 0
-        if time.perf_counter() - t0 >= seconds:
-            break
+    osc.render_rows(cam, params, r0, r0 + band, rgba, depth)
+    per_row = max((time.perf_counter() - t0) / band, 1e-6)
+    whole = per_row * h <= seconds / 3
+    samples = rows = frames = 0
+    t0 = time.perf_counter()
+    if whole:
+        while True:
+            samples += osc.render_rows(cam, params, 0, h, rgba, depth)
+            rows += h
+            frames += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
+        what = f"{frames} whole {w}x{h} frames"
+    else:
+        row = r0
+        while True:
+            a = row % h
+            b = min(a + band, h)
+            samples += osc.render_rows(cam, params, a, b, rgba, depth)
+            rows += b - a
+            row = b if b < h else 0
+            if time.perf_counter() - t0 >= seconds:
+                break
+        what = f"{rows} of {h} image rows in bands of {band} from the centre row"
     dt = time.perf_counter() - t0
-    return {"value": samples / dt / 1e9, "unit": UNIT, "cores": O.num_threads(32), "kind": "port",
-            "sample": f"{rows} of {h} image rows (central bands) of the same view, "
-                      f"{samples} samples in {dt:.1f} s, FP32 OpenMP port of the oracle"}, osc
+    return {"value": samples / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{what} of the same view, {samples} samples in {dt:.1f} s; FP32 OpenMP "
+                      "port of the oracle (camera, LUT and sample distance set up by the oracle)"}
 
 
 def _timed(fn, stream, reps):
@@ -236,8 +308,10 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
     pk = peaks()
     alg = n * 160 + size * size * BYTES_PER_PIXEL
     sc.close()
-    acc = accuracy(dev, wl, [cam], p, rows=(size // 2 - 8, size // 2 + 8))
-    cpu, _ = cpu_sample(wl, cam, p, 5.0)
+    ocam, op = oracle_setup(wl)
+    acc = accuracy(dev, wl, [cam], p, [ocam], op)
+    acc["pixels_fraction"] = acc["pixels_checked"] / (size * size)
+    cpu = cpu_sample(wl, 5.0)
     return {"workload": wl.name, "cells": n_cells ** 3, "samples_per_frame": n,
             "error_vs_fp64_oracle": acc,
             "gsamples_per_s": n / ms / 1e6, "fps": 1e3 / ms, "ms_per_frame": ms,
@@ -259,6 +333,7 @@ def bench_batch(dev, reps=5):
     from ascent_gb300 import tune
     from ascent_gb300 import volume as V
     from ascent_gb300 import workloads as W
+    from oracle import oracle as O
     wl = W.cinema_batch()
     cams = S.cinema_cameras(wl.bounds, wl.phi_theta)
     p = V.workload_params(wl)
@@ -290,8 +365,13 @@ def bench_batch(dev, reps=5):
     same = bool(torch.equal(ref, out[0]))
     builds = sc.batch_graph_builds
     sc.close()
-    acc = accuracy(dev, wl, [cams[0], cams[27]], p, rows=(h // 2 - 32, h // 2 + 32))
-    cpu, _ = cpu_sample(wl, cams[0], p, 5.0)
+    # every fourth view, whole images: a quarter of the batch's pixels
+    picks = list(range(0, v, 4))
+    _, op = oracle_setup(wl)
+    ocams = O.cinema_cameras(wl.bounds, [wl.phi_theta[i] for i in picks])
+    acc = accuracy(dev, wl, [cams[i] for i in picks], p, ocams, op)
+    acc["pixels_fraction"] = acc["pixels_checked"] / (v * h * w)
+    cpu = cpu_sample(wl, 5.0, camera=wl.phi_theta[0])
     cpu_images = cpu["value"] * 1e9 / (n / v)
     return {"workload": wl.name, "domains": len(wl.domains), "views": v, "image": [w, h],
             "cpu_port_images_per_s": cpu_images, "cpu_cores": cpu["cores"],
@@ -345,18 +425,24 @@ def bench_diff(dev, n=128, views=16, size=256, reps=5):
     fwd_ms = _timed(fwd, stream, reps)
     train_ms = _timed(fwd_train, stream, reps)
     fb_ms = _timed(fwd_bwd, stream, reps)
-    from ascent_gb300 import _native as N
     from oracle import oracle as O
-    p = N.make_params(size, size, sd, wl.scalar_range, lut.cpu().numpy(), lut_filter=N.LUT_LINEAR,
-                      alpha_cull=0.0, early_term=1.0)
+    # a quarter of the views, whole images, against the FP64 oracle with its
+    # own cameras and sample distance
+    picks = list(range(0, views, 4))
+    p = O.make_params(size, size, O.sample_distance(wl.bounds, int(np.ceil(np.sqrt(3) * (n - 1) / 0.5))),
+                      wl.scalar_range, lut.cpu().numpy(), lut_filter=O.LUT_LINEAR, alpha_cull=0.0,
+                      early_term=1.0)
+    ocams = O.cinema_cameras(wl.bounds, W.cinema_angles(side, views // side)[picks])
     osc = O.OracleScene(64)
     osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
     with torch.no_grad():
-        img = D.render(gt, lut, cams[:2], d.origin, d.spacing, size, size, sd, wl.scalar_range).cpu().numpy()
-    errs = [_err(img[i], osc.render(cams[i], p)[0]) for i in range(2)]
+        img = D.render(gt, lut, [cams[i] for i in picks], d.origin, d.spacing, size, size, sd,
+                       wl.scalar_range).cpu().numpy()
+    errs = [_err(img[k], osc.render(ocams[k], p)[0]) for k in range(len(picks))]
     acc = {k: max(e[k] for e in errs) if k != "frac_within_2_255" else min(e[k] for e in errs)
            for k in errs[0]}
-    acc.update({"views": 2, "oracle": "FP64 CPU oracle (oracle/gvr_oracle.c), linear LUT, no cull"})
+    acc.update({"views": len(picks), "pixels_fraction": len(picks) / views,
+                "oracle": "FP64 CPU oracle (oracle/gvr_oracle.c), linear LUT, no cull, set up by the oracle"})
     return {"workload": f"diff{n}^3x{views}views@{size}x{size}", "lut": 256, "checkpoint_every": 64,
             "error_vs_fp64_oracle": acc,
             "fwd_ms": fwd_ms, "fwd_train_ms": train_ms, "fwd_bwd_ms": fb_ms,
@@ -373,29 +459,25 @@ def _err(g, o) -> dict:
             "frac_over_4_255": float((d > 4 / 255).any(axis=-1).mean())}
 
 
-def accuracy(dev, wl, cams, params, rows=None, precision=64) -> dict:
+def accuracy(dev, wl, cams, params, oracle_cams, oracle_params, rows=None, precision=64) -> dict:
     """Error of the GPU images against the FP64 oracle on the same inputs,
-    over image rows [rows[0], rows[1]) (the whole image when None)."""
+    over image rows [rows[0], rows[1]) (the whole image when None). The GPU
+    renders with the product's cameras and parameters, the oracle with its
+    own (oracle_setup), so the set-up is compared too."""
     from ascent_gb300 import scene as S
     from ascent_gb300 import volume as V
-    from oracle import oracle as O
-    osc = O.OracleScene(precision)
-    for d in wl.domains:
-        if hasattr(d, "conn"):
-            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
-        else:
-            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    osc = oracle_scene_of(wl, precision)
     h, w = params.height, params.width
     r0, r1 = rows if rows else (0, h)
     out = []
     with S.Scene(dev) as sc:
         V.load_workload(sc, wl)
-        for cam in cams:
+        for cam, ocam in zip(cams, oracle_cams):
             g, _ = sc.render(cam, params)
             o = np.zeros((h, w, 4), np.float32)
             dep = np.zeros((h, w), np.float32)
             t0 = time.perf_counter()
-            osc.render_rows(cam, params, r0, r1, o, dep)
+            osc.render_rows(ocam, oracle_params, r0, r1, o, dep)
             e = _err(g[r0:r1], o[r0:r1])
             e["oracle_s"] = round(time.perf_counter() - t0, 2)
             out.append(e)
@@ -403,7 +485,9 @@ def accuracy(dev, wl, cams, params, rows=None, precision=64) -> dict:
              for k in ("max", "mae", "frac_within_2_255", "frac_over_4_255")}
     worst["rows"] = [r0, r1]
     worst["views"] = len(cams)
-    worst["oracle"] = "FP64 CPU oracle (oracle/gvr_oracle.c)"
+    worst["pixels_checked"] = len(cams) * (r1 - r0) * w
+    worst["oracle_s"] = round(sum(e["oracle_s"] for e in out), 1)
+    worst["oracle"] = "FP64 CPU oracle (oracle/gvr_oracle.c), set up by the oracle"
     return worst
 
 
@@ -496,58 +580,63 @@ def bench_plain_small(dev, reps=20) -> dict:
         for _ in range(3):
             N.call("gvr_render_volume", *args)
         ms = _timed(lambda: N.call("gvr_render_volume", *args), stream, reps)
-    cpu, _ = cpu_sample(wl, cam, p, 3.0)
+    cpu = cpu_sample(wl, 3.0)
+    ocam, op = oracle_setup(wl)
     return {"workload": wl.name, "samples_per_frame": n, "gsamples_per_s": n / ms / 1e6,
             "fps": 1e3 / ms, "ms_per_frame": ms, "cpu_port_gsamples_per_s": cpu["value"],
             "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
-            "error_vs_fp64_oracle": accuracy(dev, wl, [cam], p)}
+            "error_vs_fp64_oracle": accuracy(dev, wl, [cam], p, [ocam], op)}
 
 
 def run_reference(args):
-    """CPU implementation of the path (the oracle's FP32 OpenMP port) on this host."""
+    """The CPU implementation of the path on this host (rank 0 only): the
+    oracle's FP32 OpenMP port, set up by the oracle's own functions, on all
+    host threads. A step is one whole frame of the workload; when the run
+    would take over three minutes that way, a step is a band of rows (at
+    least four per thread) sized to fit. Neither the product package nor its
+    library is loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    from ascent_gb300 import volume as V
-    wl, _ = setup_workload(args)
-    cam = V.workload_camera(wl)
-    params, _ = bench_params(wl)
     from oracle import oracle as O
-    osc = O.OracleScene(32)
-    for d in wl.domains:
-        if hasattr(d, "conn"):
-            osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
-        else:
-            osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    wl, _ = setup_workload(args)
+    cam, params = oracle_setup(wl, float_lut=True)
+    osc = oracle_scene_of(wl, 32)
+    cores = O.num_threads(32)
     h, w = params.height, params.width
     rgba = np.zeros((h, w, 4), np.float32)
     depth = np.zeros((h, w), np.float32)
-    budget = min(2.0, 150.0 / max(1, args.steps + args.warmup))
-    # calibrate a band height that takes about `budget` seconds
+    # the first warm-up frame doubles as the estimate of a frame's time
     t0 = time.perf_counter()
-    osc.render_rows(cam, params, h // 2 - 2, h // 2 + 2, rgba, depth)
-    per_row = max((time.perf_counter() - t0) / 4, 1e-4)
-    band = int(max(1, min(h, budget / per_row)))
-    r0 = max(0, h // 2 - band // 2)
-    for _ in range(args.warmup):
-        osc.render_rows(cam, params, r0, r0 + band, rgba, depth)
+    osc.render_rows(cam, params, 0, h, rgba, depth)
+    frame_s = time.perf_counter() - t0
+    budget = 180.0
+    runs = args.steps + max(args.warmup - 1, 0)
+    if frame_s * runs <= budget:
+        r0, r1 = 0, h
+    else:
+        band = int(min(h, max(4 * cores, h * budget / (frame_s * runs))))
+        r0 = max(0, h // 2 - band // 2)
+        r1 = r0 + band
+    for _ in range(max(args.warmup - 1, 0)):
+        osc.render_rows(cam, params, r0, r1, rgba, depth)
     total = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        total += osc.render_rows(cam, params, r0, r0 + band, rgba, depth)
+        total += osc.render_rows(cam, params, r0, r1, rgba, depth)
     dt = time.perf_counter() - t0
     value = total / dt / 1e9
-    cores = O.num_threads(32)
+    sample = (f"whole {w}x{h} frames, one per step" if (r0, r1) == (0, h) else
+              f"rows {r0}..{r1} of {h} per step (whole frames would exceed {budget:.0f} s)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": wl.name, "domains": len(wl.domains), "image": [w, h],
-                       "samples_param": wl.samples, "step_sample_rows": [r0, r0 + band]},
+            "data": "synthetic", "config": bench_config(wl, args),
+            "samples_per_step": total // max(args.steps, 1),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"rows {r0}..{r0 + band} of {h} per step; the reference's "
-                                       "VTK-m renderer is not buildable here, this is the oracle's "
-                                       "FP32 OpenMP port of the same algorithm"},
+                             "sample": sample + "; the reference's VTK-m renderer cannot be built "
+                                       "here, this is the oracle's FP32 OpenMP port of the same "
+                                       "algorithm, set up by the oracle"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -727,13 +816,14 @@ def run_ours(args):
     field_bytes = sum(d.field.nbytes for d in wl.domains)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        cpu, _ = cpu_sample(wl, cam, params, args.cpu_seconds)
+        cpu = cpu_sample(wl, args.cpu_seconds, float_lut=True)
     scene.close()
     others = {}
     main_acc = None
     if world == 1 and not args.no_configs:
         torch.cuda.synchronize()
-        main_acc = accuracy(dev, wl, [cam], params)
+        ocam, oparams = oracle_setup(wl, float_lut=True)
+        main_acc = accuracy(dev, wl, [cam], params, [ocam], oparams)
         others["ingest"] = bench_ingest(dev, wl)
         others["plain_64"] = bench_plain_small(dev)
         others["hex"] = bench_hex(dev)
@@ -745,17 +835,10 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "fps": 1e3 * args.steps / total_ms,
-        "config": {"workload": wl.name, "grid_nodes": args.cells + 1, "domains": len(wl.domains),
-                   "image": [wl.width, wl.height], "samples_param": wl.samples,
-                   "sample_dist": params.sample_dist, "samples_per_frame": n_samples,
-                   "early_term": params.early_term,
-                   "lut": "1024-entry float LUT for both arms; the reference's multi-domain "
-                          "uint8 LUT would round opacity to 0 below s=0.98 at 1774 samples",
-                   "l2": f"inputs {bricked_bytes(wl) / 2**20:.0f} MiB bricked > 129 MB L2; "
-                         "not flushed",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "tuning": tuning["best"], "tuning_ms": tuning["ms"],
-                   "generate_s": round(gen_s, 2)},
+        "config": bench_config(wl, args),
+        "samples_per_step": n_samples, "sample_dist": params.sample_dist,
+        "parallelism": "replicas" if world > 1 else "single GPU",
+        "tuning": {"best": tuning["best"], "ms": tuning["ms"]}, "generate_s": round(gen_s, 2),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                      "peak_source": pk["source"], "traffic_workload": traffic_wl,

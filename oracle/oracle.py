@@ -19,7 +19,52 @@ from pathlib import Path
 
 import numpy as np
 
-from ascent_gb300._native import Camera, ColorTable, RenderParams, dptr, fptr
+# ctypes mirrors of the gvr.h structs the oracle's C entry points take. They
+# are declared here, not imported from the product package, so that the CPU
+# arm of the benchmark never maps the product library. Structures of the
+# same layout built elsewhere (the product binding's) are accepted too: the
+# entry points take their address.
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("look_at", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_y", C.c_float), ("zoom", C.c_float), ("xpan", C.c_float), ("ypan", C.c_float),
+                ("near_plane", C.c_float), ("far_plane", C.c_float)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("sample_dist", C.c_float),
+                ("scalar_min", C.c_float), ("scalar_max", C.c_float),
+                ("lut_rgba", C.POINTER(C.c_float)), ("lut_size", C.c_int), ("lut_filter", C.c_int),
+                ("alpha_cull", C.c_float), ("early_term", C.c_float), ("quantize_uint8", C.c_int),
+                ("render_bg", C.c_int), ("bg_color", C.c_float * 4), ("clear_depth", C.c_float)]
+
+
+class ColorTable(C.Structure):
+    _fields_ = [("n_rgb", C.c_int), ("rgb_pos", C.POINTER(C.c_double)), ("rgb", C.POINTER(C.c_double)),
+                ("n_alpha", C.c_int), ("alpha_pos", C.POINTER(C.c_double)),
+                ("alpha", C.POINTER(C.c_double))]
+
+
+LUT_NEAREST, LUT_LINEAR = 0, 1
+UINT8_NONE, UINT8_ROUND, UINT8_TRUNCATE = 0, 1, 2
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _addr(obj, kind) -> int:
+    """Address of a struct laid out as `kind` (this module's or a same-layout mirror)."""
+    if not isinstance(obj, C.Structure) or C.sizeof(obj) != C.sizeof(kind) or \
+            [f[0] for f in type(obj)._fields_] != [f[0] for f in kind._fields_]:
+        raise TypeError(f"expected a {kind.__name__} structure, got {type(obj).__name__}")
+    return C.addressof(obj)
+
 
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
@@ -53,12 +98,14 @@ def load(precision: int = 64) -> C.CDLL:
     lib.or_correct_opacity.argtypes = [P(d), i, i, P(d)]
     lib.or_sample_distance.argtypes = [P(d), i]
     lib.or_sample_distance.restype = f
-    lib.or_color_table_sample.argtypes = [P(ColorTable), i, i, P(f)]
-    lib.or_camera_reset_to_bounds.argtypes = [P(Camera), P(d)]
-    lib.or_camera_azimuth.argtypes = [P(Camera), d]
-    lib.or_camera_elevation.argtypes = [P(Camera), d]
-    lib.or_cinema_cameras.argtypes = [P(d), P(f), i, P(Camera)]
-    lib.or_visibility_order.argtypes = [P(Camera), P(d), i, P(i)]
+    # struct arguments are passed by address (void *): a Camera, RenderParams
+    # or ColorTable of this module or any structure of the same layout
+    lib.or_color_table_sample.argtypes = [vp, i, i, P(f)]
+    lib.or_camera_reset_to_bounds.argtypes = [vp, P(d)]
+    lib.or_camera_azimuth.argtypes = [vp, d]
+    lib.or_camera_elevation.argtypes = [vp, d]
+    lib.or_cinema_cameras.argtypes = [P(d), P(f), i, vp]
+    lib.or_visibility_order.argtypes = [vp, P(d), i, P(i)]
     lib.or_composite_partials.argtypes = [i, P(i), vp, vp]
     lib.or_scene_new.restype = vp
     lib.or_scene_free.argtypes = [vp]
@@ -67,9 +114,9 @@ def load(precision: int = 64) -> C.CDLL:
     lib.or_scene_add_hex.argtypes = [vp, C.c_int64, P(f), P(f), P(f), C.c_int64, P(i), P(f), i]
     lib.or_hex_bvh.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
     lib.or_hex_locate.argtypes = [vp, i, P(f), i, P(i), P(f)]
-    lib.or_render.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
-    lib.or_render_rows.argtypes = [vp, P(Camera), P(RenderParams), i, i, P(f), P(f), P(C.c_uint64)]
-    lib.or_render_over.argtypes = [vp, P(Camera), P(RenderParams), P(f), P(f), P(C.c_uint64)]
+    lib.or_render.argtypes = [vp, vp, vp, P(f), P(f), P(C.c_uint64)]
+    lib.or_render_rows.argtypes = [vp, vp, vp, i, i, P(f), P(f), P(C.c_uint64)]
+    lib.or_render_over.argtypes = [vp, vp, vp, P(f), P(f), P(C.c_uint64)]
     lib.or_num_threads.restype = i
     _libs[precision] = lib
     return lib
@@ -150,8 +197,8 @@ class OracleScene:
         rgba = np.zeros((h, w, 4), dtype=np.float32)
         depth = np.zeros((h, w), dtype=np.float32)
         n = C.c_uint64(0)
-        rc = self.lib.or_render(self.handle, C.byref(cam), C.byref(params), fptr(rgba), fptr(depth),
-                                C.byref(n))
+        rc = self.lib.or_render(self.handle, _addr(cam, Camera), _addr(params, RenderParams),
+                                fptr(rgba), fptr(depth), C.byref(n))
         if rc != 0:
             raise RuntimeError(f"oracle render failed with status {rc}")
         return rgba, depth, int(n.value)
@@ -161,8 +208,8 @@ class OracleScene:
         rgba = np.array(canvas_rgba, dtype=np.float32, copy=True, order="C")
         depth = np.array(canvas_depth, dtype=np.float32, copy=True, order="C")
         n = C.c_uint64(0)
-        rc = self.lib.or_render_over(self.handle, C.byref(cam), C.byref(params), fptr(rgba), fptr(depth),
-                                     C.byref(n))
+        rc = self.lib.or_render_over(self.handle, _addr(cam, Camera), _addr(params, RenderParams),
+                                     fptr(rgba), fptr(depth), C.byref(n))
         if rc != 0:
             raise RuntimeError(f"oracle render failed with status {rc}")
         return rgba, depth, int(n.value)
@@ -170,8 +217,8 @@ class OracleScene:
     def render_rows(self, cam: Camera, params: RenderParams, row0: int, row1: int, rgba, depth) -> int:
         """Render rows [row0, row1) into caller buffers; returns the sample count."""
         n = C.c_uint64(0)
-        rc = self.lib.or_render_rows(self.handle, C.byref(cam), C.byref(params), int(row0), int(row1),
-                                     fptr(rgba), fptr(depth), C.byref(n))
+        rc = self.lib.or_render_rows(self.handle, _addr(cam, Camera), _addr(params, RenderParams),
+                                     int(row0), int(row1), fptr(rgba), fptr(depth), C.byref(n))
         if rc != 0:
             raise RuntimeError(f"oracle render failed with status {rc}")
         return int(n.value)
@@ -276,3 +323,116 @@ def hex_face_neighbors(conn) -> np.ndarray:
 
 def num_threads(precision: int = 32) -> int:
     return int(load(precision).or_num_threads())
+
+
+# ---------------------------------------------------------------------------
+# Render set-up restated on the oracle side: the camera, the opacity-corrected
+# and sampled transfer function and the sample distance of a volume plot,
+# built with the oracle's own C functions (never the product library's), so
+# that a fault in the product's host set-up shows up as an image difference.
+# ---------------------------------------------------------------------------
+
+LUT_SIZE = 1024   # detail::convert_table samples 1024 entries (VolumeRenderer.cpp:65-90)
+
+
+def correct_opacity(alpha, num_samples: int) -> np.ndarray:
+    """VolumeRenderer::CorrectOpacity (VolumeRenderer.cpp:448-466)."""
+    a = np.ascontiguousarray(alpha, dtype=np.float64)
+    out = np.empty_like(a)
+    if load(64).or_correct_opacity(dptr(a), a.size, int(num_samples), dptr(out)) != 0:
+        raise ValueError("samples must be greater than 0")
+    return out
+
+
+def sample_distance(bounds, num_samples: int) -> float:
+    """VolumeRenderer::PreExecute (VolumeRenderer.cpp:600-612)."""
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    return float(load(64).or_sample_distance(dptr(b), int(num_samples)))
+
+
+def color_table_sample(rgb_pos, rgb, alpha_pos, alpha, n: int = LUT_SIZE,
+                       uint8_mode: int = UINT8_NONE) -> np.ndarray:
+    """Sample control points to an (n, 4) float32 RGBA table; through uint8
+    for the multi-domain path (VolumeRenderer.cpp:65-90)."""
+    keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (rgb_pos, rgb, alpha_pos, alpha)]
+    t = ColorTable(len(keep[0]), dptr(keep[0]), dptr(keep[1]), len(keep[2]), dptr(keep[2]),
+                   dptr(keep[3]))
+    out = np.zeros((n, 4), np.float32)
+    if load(64).or_color_table_sample(C.byref(t), int(n), int(uint8_mode), fptr(out)) != 0:
+        raise ValueError("invalid colour table")
+    return out
+
+
+def camera_reset_to_bounds(bounds) -> Camera:
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    cam = Camera()
+    load(64).or_camera_reset_to_bounds(C.byref(cam), dptr(b))
+    return cam
+
+
+def cinema_cameras(bounds, phi_theta) -> list:
+    """CinemaManager::create_cinema_cameras (rendering_filters.cpp:906-960)."""
+    b = np.ascontiguousarray(bounds, dtype=np.float64)
+    pt = np.ascontiguousarray(phi_theta, dtype=np.float32).reshape(-1, 2)
+    out = (Camera * max(len(pt), 1))()
+    load(64).or_cinema_cameras(dptr(b), fptr(pt), len(pt), out)
+    cams = []
+    for i in range(len(pt)):
+        c = Camera()
+        C.memmove(C.byref(c), C.byref(out[i]), C.sizeof(Camera))
+        cams.append(c)
+    return cams
+
+
+def workload_camera(wl) -> Camera:
+    """Reset to the scene bounds, then azimuth, then elevation (the order
+    parse_camera applies them, conduit_to_vtkm_parsing.cpp:164-174)."""
+    cam = camera_reset_to_bounds(wl.bounds)
+    if wl.azimuth:
+        load(64).or_camera_azimuth(C.byref(cam), float(wl.azimuth))
+    if wl.elevation:
+        load(64).or_camera_elevation(C.byref(cam), float(wl.elevation))
+    return cam
+
+
+def make_params(width, height, sample_dist, scalar_range, lut, *, lut_filter=LUT_NEAREST,
+                alpha_cull=0.001, early_term=0.99, quantize_uint8=False, render_bg=False,
+                bg_color=(0.0, 0.0, 0.0, 1.0), clear_depth=1.0) -> RenderParams:
+    """RenderParams for the oracle; the LUT array is kept alive by the struct."""
+    lut = np.ascontiguousarray(lut, dtype=np.float32).reshape(-1, 4)
+    p = RenderParams()
+    p.width, p.height = int(width), int(height)
+    p.sample_dist = float(sample_dist)
+    p.scalar_min, p.scalar_max = float(scalar_range[0]), float(scalar_range[1])
+    p.lut_rgba = fptr(lut)
+    p.lut_size = lut.shape[0]
+    p.lut_filter = int(lut_filter)
+    p.alpha_cull = float(alpha_cull)
+    p.early_term = float(early_term)
+    p.quantize_uint8 = int(bool(quantize_uint8))
+    p.render_bg = int(bool(render_bg))
+    for i in range(4):
+        p.bg_color[i] = float(bg_color[i])
+    p.clear_depth = float(clear_depth)
+    p._lut_keepalive = lut  # noqa: SLF001
+    return p
+
+
+def workload_lut(wl, single_domain: bool | None = None) -> np.ndarray:
+    """The plot's LUT: control points opacity-corrected for wl.samples, sampled
+    at 1024 entries, in float on the one-domain path and through uint8
+    (rounded) on the multi-domain path (VolumeRenderer.cpp:469-597, 65-90)."""
+    single = wl.single_domain if single_domain is None else single_domain
+    alpha = correct_opacity(wl.alpha, wl.samples)
+    return color_table_sample(wl.rgb_pos, wl.rgb, wl.alpha_pos, alpha, LUT_SIZE,
+                              UINT8_NONE if single else UINT8_ROUND)
+
+
+def workload_params(wl, *, lut=None, single_domain: bool | None = None, **kw) -> RenderParams:
+    """Render parameters of a workload's volume plot, set up by the oracle."""
+    single = wl.single_domain if single_domain is None else single_domain
+    if lut is None:
+        lut = workload_lut(wl, single)
+    kw.setdefault("quantize_uint8", single)
+    return make_params(wl.width, wl.height, sample_distance(wl.bounds, wl.samples), wl.scalar_range,
+                       lut, **kw)

@@ -10,7 +10,7 @@ from ascent_gb300 import png as PNG
 from ascent_gb300 import scene as S
 from ascent_gb300 import volume as V
 from ascent_gb300 import workloads as W
-from golden.make_golden import decode_png
+from ascent_gb300.png import decode_png
 
 pytestmark = pytest.mark.gpu
 

@@ -91,7 +91,8 @@ def test_hex_render_matches_oracle():
     d = wl.domains[0]
     osc = O.OracleScene(64)
     osc.add_hex(d.x, d.y, d.z, d.conn, d.field)
-    o, od, on = osc.render(cam, p)
+    # the oracle's camera and parameters come from its own set-up functions
+    o, od, on = osc.render(O.workload_camera(wl), O.workload_params(wl))
     assert o[..., 3].max() > 0.1
     assert_parity(g, o)
     assert abs(gn - on) <= 1e-3 * on
