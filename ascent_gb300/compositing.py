@@ -5,8 +5,10 @@
 `composite(partial_images)` takes a list of per-image partial arrays and
 returns one record per pixel, blended front to back in depth order, in the
 reference's output order (single-record pixels first, then blended pixels,
-each in pixel order). The work runs in gvr_composite_partials (device radix
-sort, segment scans and an FP32 blend kernel).
+each in pixel order). The work runs in gvr_composite_partials: records are
+grouped by pixel with a histogram of pixel ids and a bucket scatter (a
+device radix sort when the ids are sparse), each pixel's records are ordered
+by (depth, input position) and blended in FP32 by one thread per pixel.
 
 Host partials are numpy structured arrays of `PARTIAL_DTYPE` (the 24-byte
 VolumePartial<float> record). Device partials are torch int32 tensors of

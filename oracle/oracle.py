@@ -13,7 +13,6 @@ and, when the reference sources are present at build time,
 from __future__ import annotations
 
 import ctypes as C
-import os
 import subprocess
 from pathlib import Path
 
@@ -69,7 +68,6 @@ def _addr(obj, kind) -> int:
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF = HERE / "_ref"
-REFERENCE_ROOT = Path(os.environ.get("GVR_REFERENCE_ROOT", "/root/reference"))
 
 PARTIAL_DTYPE = np.dtype([("pixel_id", "<i4"), ("depth", "<f4"), ("rgb", "<f4", (3,)),
                           ("alpha", "<f4")])
@@ -78,12 +76,13 @@ _libs: dict = {}
 
 
 def build(with_reference: bool | None = None) -> None:
-    """make the oracle; also the apcomp reference when its sources exist."""
+    """make the oracle; also the apcomp reference when its sources exist
+    (oracle/Makefile's REF, overridden by GVR_REFERENCE_ROOT)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
     if with_reference is None:
-        with_reference = (REFERENCE_ROOT / "src/libs/apcomp/partial_compositor.cpp").exists()
-    if with_reference:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref-if-present"], check=True)
+    elif with_reference:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
 
 
 def load(precision: int = 64) -> C.CDLL:
