@@ -105,6 +105,9 @@ _SIGS = {
     "gvr_last_error": (C.c_char_p, []),
     "gvr_version": (C.c_int, []),
     "gvr_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
+    "gvr_scratch_trim": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gvr_zbuffer_composite": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int,
+                                        C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "gvr_correct_opacity": (C.c_int, [C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "gvr_sample_distance": (C.c_int, [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_float)]),
     "gvr_color_table_sample": (C.c_int, [C.POINTER(ColorTable), C.c_int, C.c_int, C.POINTER(C.c_float)]),
@@ -195,3 +198,11 @@ def launch_count() -> int:
     n = C.c_uint64(0)
     call("gvr_launch_count", C.byref(n))
     return int(n.value)
+
+
+def scratch_trim(device: int = 0, keep_bytes: int = 0) -> int:
+    """Return the library's pooled scratch on `device` to the system down to
+    keep_bytes (gvr_scratch_trim); the bytes still reserved."""
+    r = C.c_uint64(0)
+    call("gvr_scratch_trim", int(device), int(keep_bytes), C.byref(r))
+    return int(r.value)

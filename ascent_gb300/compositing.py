@@ -89,3 +89,45 @@ class PartialCompositor:
         images = [np.asarray(p, dtype=PARTIAL_DTYPE) for p in partial_images]
         merged = np.concatenate(images) if images else np.zeros(0, PARTIAL_DTYPE)
         return composite_partials(merged)
+
+
+def zbuffer_composite(rgba_images, depth_images, stream=None):
+    """Z-buffer compositing of opaque canvases (gvr_zbuffer_composite):
+    Renderer::Composite in Z_BUFFER_SURFACE mode (vtkh/rendering/
+    Renderer.cpp:111-142, ImageCompositor.hpp:49-76). Inputs are lists of
+    (H, W, 4) / (H, W) float32 arrays, all numpy (host) or all CUDA tensors
+    (device, stream-ordered on `stream` or the current stream); returns the
+    composited (rgba, depth) on the same side. The result is the opaque
+    canvas a volume pass draws over (Scene.render_over)."""
+    n = len(rgba_images)
+    if n == 0 or n != len(depth_images):
+        raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "need as many depth images as colour images (>= 1)")
+    on_device = not isinstance(rgba_images[0], np.ndarray)
+    if on_device:
+        import torch
+        cols = [c.contiguous() for c in rgba_images]
+        deps = [d.contiguous() for d in depth_images]
+        if any(c.dtype != torch.float32 or not c.is_cuda for c in cols + deps):
+            raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "device images must be float32 CUDA tensors")
+        h, w = cols[0].shape[0], cols[0].shape[1]
+        if any(tuple(c.shape) != (h, w, 4) for c in cols) or any(tuple(d.shape) != (h, w) for d in deps):
+            raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "images must share one (H, W) size")
+        out = torch.empty_like(cols[0])
+        out_d = torch.empty_like(deps[0])
+        cp = (C.c_void_p * n)(*[c.data_ptr() for c in cols])
+        dp = (C.c_void_p * n)(*[d.data_ptr() for d in deps])
+        N.call("gvr_zbuffer_composite", n, cp, dp, w, h, C.c_void_p(out.data_ptr()),
+               C.c_void_p(out_d.data_ptr()), N.MEM_DEVICE, C.c_void_p(_stream_ptr(stream)))
+        return out, out_d
+    cols = [np.ascontiguousarray(c, dtype=np.float32) for c in rgba_images]
+    deps = [np.ascontiguousarray(d, dtype=np.float32) for d in depth_images]
+    h, w = cols[0].shape[0], cols[0].shape[1]
+    if any(c.shape != (h, w, 4) for c in cols) or any(d.shape != (h, w) for d in deps):
+        raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "images must share one (H, W) size")
+    out = np.zeros((h, w, 4), np.float32)
+    out_d = np.zeros((h, w), np.float32)
+    cp = (C.c_void_p * n)(*[c.ctypes.data for c in cols])
+    dp = (C.c_void_p * n)(*[d.ctypes.data for d in deps])
+    N.call("gvr_zbuffer_composite", n, cp, dp, w, h, C.c_void_p(out.ctypes.data),
+           C.c_void_p(out_d.ctypes.data), N.MEM_HOST, None)
+    return out, out_d

@@ -80,6 +80,31 @@ cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream)
   return cudaMallocFromPoolAsync(ptr, bytes, pool, stream);
 }
 
+}  // namespace gvr
+
+int gvr_scratch_trim(int device, uint64_t keep_bytes, uint64_t *reserved_out)
+{
+  using namespace gvr;
+  if (device < 0) return set_error(GVR_ERR_INVALID_ARGUMENT, "negative device");
+  cudaMemPool_t pool = nullptr;
+  if (device < kMaxPoolDevices) {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    pool = g_pools[device];
+  }
+  uint64_t reserved = 0;
+  if (pool) {
+    // blocks still in use are kept whatever keep_bytes says; memory freed
+    // on a stream is returned once that free has completed
+    cudaError_t e = cudaMemPoolTrimTo(pool, (size_t)keep_bytes);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMemPoolTrimTo");
+    e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+    if (e != cudaSuccess) return cuda_error(e, "cudaMemPoolGetAttribute");
+  }
+  if (reserved_out) *reserved_out = reserved;
+  return GVR_OK;
+}
+
+namespace gvr {
 namespace {
 
 struct V3 {
@@ -479,7 +504,14 @@ static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, i
                            d.d_cells, d.range, d.stg, 0);
   }
   if (e != cudaSuccess) return cuda_error(e, "field upload");
-  if (timed_out) return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
+  s->table_dirty = true;
+  s->classify_valid = false;
+  if (timed_out) {
+    // the bricks were rewritten with non-finite ranges: the domain's range
+    // is unknown until the field is published again
+    d.range[0] = d.range[1] = std::nan("");
+    return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
+  }
   if (!(std::isfinite(d.range[0]) && std::isfinite(d.range[1])))
     return set_error(GVR_ERR_INVALID_ARGUMENT, "field contains non-finite values");
   s->table_dirty = true;
@@ -725,8 +757,15 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
     e = cudaMemcpyAsync(s->h_ranges, s->d_ranges, sizeof(float2) * (n + 1), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "field ranges");
-    if (reinterpret_cast<const int *>(s->h_ranges + n)[0] != 0)
+    if (reinterpret_cast<const int *>(s->h_ranges + n)[0] != 0) {
+      // some bricks were rewritten with non-finite ranges: the ranges of
+      // this call's domains are unknown until they are published again
+      for (int k = 0; k < n; ++k) {
+        Domain &d = s->domains[domain_ids[k]];
+        if (piped(d)) d.range[0] = d.range[1] = std::nan("");
+      }
       return set_error(GVR_ERR_TIMEOUT, "field staging copy did not complete");
+    }
     bool bad = false;
     for (int k = 0; k < n; ++k) {
       Domain &d = s->domains[domain_ids[k]];
@@ -806,6 +845,11 @@ int gvr_scene_range(const gvr_scene *s, double r[2])
   r[0] = INFINITY;
   r[1] = -INFINITY;
   for (const Domain &d : s->domains) {
+    if (!(std::isfinite(d.range[0]) && std::isfinite(d.range[1]))) {
+      // a domain whose field publish did not complete: range unknown
+      r[0] = r[1] = std::nan("");
+      return GVR_OK;
+    }
     r[0] = std::min(r[0], d.range[0]);
     r[1] = std::max(r[1], d.range[1]);
   }

@@ -8,6 +8,16 @@
 // streams W*H*20 bytes; the deflate of the PNG itself stays on the host.
 // Values are clamped to [0, 255] before the truncation (the reference's cast
 // of an out-of-range float is undefined; the canvas holds values in [0, 1]).
+//
+// Also here: the Z-buffer compositing of opaque canvases (surface plots
+// rendered per domain or per plot) that Renderer::Composite does in
+// Z_BUFFER_SURFACE mode before the volume pass draws over the result
+// (Renderer.cpp:111-142, Compositor.cpp:86-125, ImageCompositor.hpp:49-76,
+// Image.hpp:80-113, Renderer::ImageToCanvas :271-289). One thread per pixel
+// walks the images in order: each image's colour goes through the 8-bit
+// vtkh::Image (truncation), its depth through |depth|; image i > 0 replaces
+// the kept pixel where its depth is <= 1 and not behind the kept depth; the
+// kept 8-bit colour comes back as value / 255 with its depth.
 #include <cstdint>
 
 #include "gvr_internal.h"
@@ -30,10 +40,107 @@ rgba8_kernel(const float4 *__restrict__ rgba, int width, int height, uchar4 *__r
   }
 }
 
+constexpr int kMaxZImages = 64;
+
+struct ZImages {
+  const float4 *rgba[kMaxZImages];
+  const float *depth[kMaxZImages];
+};
+
+__device__ __forceinline__ uchar4 to_u8(float4 v)
+{
+  auto q = [](float c) {
+    return (unsigned char)__float2uint_rz(fminf(fmaxf(c * 255.f, 0.f), 255.f));
+  };
+  return make_uchar4(q(v.x), q(v.y), q(v.z), q(v.w));
+}
+
+__global__ void __launch_bounds__(256)
+zbuffer_kernel(const ZImages images, int n_images, int64_t n, float4 *__restrict__ out_rgba,
+               float *__restrict__ out_depth)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    // Image::Init of the first image: 8-bit colour, |depth|
+    uchar4 c = to_u8(images.rgba[0][i]);
+    float d = fabsf(images.depth[0][i]);
+    for (int k = 1; k < n_images; ++k) {
+      const float dk = fabsf(images.depth[k][i]);
+      if (dk > 1.f || d < dk) continue;   // ZBufferComposite's test
+      d = dk;
+      c = to_u8(images.rgba[k][i]);
+    }
+    const float s = 1.f / 255.f;          // ImageToCanvas
+    out_rgba[i] = make_float4((float)c.x * s, (float)c.y * s, (float)c.z * s, (float)c.w * s);
+    out_depth[i] = d;
+  }
+}
+
 }  // namespace
 }  // namespace gvr
 
 using namespace gvr;
+
+extern "C" int gvr_zbuffer_composite(int n_images, const float *const *rgba,
+                                     const float *const *depth, int width, int height,
+                                     float *out_rgba, float *out_depth, int location, void *stream)
+{
+  if (n_images < 1 || n_images > kMaxZImages)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "n_images must be 1 .. 64");
+  if (!rgba || !depth || !out_rgba || !out_depth)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "image buffers are NULL");
+  for (int k = 0; k < n_images; ++k)
+    if (!rgba[k] || !depth[k]) return set_error(GVR_ERR_INVALID_ARGUMENT, "image buffers are NULL");
+  if (width < 1 || height < 1 || (int64_t)width * height > (1ll << 28))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "image size must be >= 1 and <= 2^28 pixels");
+  if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad location");
+  const int64_t pixels = (int64_t)width * height;
+  const size_t per = (size_t)pixels * (sizeof(float4) + sizeof(float));
+  cudaStream_t st = (cudaStream_t)stream;
+  ZImages im{};
+  float4 *d_out = reinterpret_cast<float4 *>(out_rgba);
+  float *d_dep = out_depth;
+  void *scratch = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (location == GVR_MEM_HOST) {
+    // inputs and output staged in one scratch block: n + 1 canvases
+    e = scratch_alloc(&scratch, per * (size_t)(n_images + 1), st);
+    if (e != cudaSuccess) return cuda_error(e, "allocate image scratch");
+    char *b = static_cast<char *>(scratch);
+    for (int k = 0; k < n_images && e == cudaSuccess; ++k) {
+      float4 *c = reinterpret_cast<float4 *>(b + per * k);
+      float *z = reinterpret_cast<float *>(c + pixels);
+      e = cudaMemcpyAsync(c, rgba[k], sizeof(float4) * pixels, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(z, depth[k], sizeof(float) * pixels, cudaMemcpyHostToDevice, st);
+      im.rgba[k] = c;
+      im.depth[k] = z;
+    }
+    d_out = reinterpret_cast<float4 *>(b + per * n_images);
+    d_dep = reinterpret_cast<float *>(d_out + pixels);
+  } else {
+    for (int k = 0; k < n_images; ++k) {
+      im.rgba[k] = reinterpret_cast<const float4 *>(rgba[k]);
+      im.depth[k] = depth[k];
+    }
+  }
+  if (e == cudaSuccess) {
+    const int grid = (int)std::min<int64_t>((pixels + 255) / 256, 152 * 8);
+    zbuffer_kernel<<<grid, 256, 0, st>>>(im, n_images, pixels, d_out, d_dep);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && location == GVR_MEM_HOST) {
+    e = cudaMemcpyAsync(out_rgba, d_out, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(out_depth, d_dep, sizeof(float) * pixels, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  if (scratch) cudaFreeAsync(scratch, st);
+  if (e != cudaSuccess) return cuda_error(e, "z-buffer composite");
+  return GVR_OK;
+}
 
 extern "C" int gvr_canvas_to_rgba8(const float *rgba, int width, int height, uint8_t *out,
                                    int location, void *stream)

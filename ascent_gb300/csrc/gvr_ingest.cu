@@ -6,6 +6,7 @@
 // Renderer::PreExecute (Renderer.cpp:144-179). The output layout is the
 // renderer's own: 8^3-cell bricks with a one-node apron plus a per-brick
 // {min,max} macrocell grid used for empty-space skipping.
+#include <cstdlib>
 #include <cfloat>
 #include <cstdint>
 #include <cstdio>
@@ -109,10 +110,10 @@ __device__ __forceinline__ bool mbar_try_wait(const uint64_t *bar, unsigned phas
   return ok != 0;
 }
 
-// Wait for phase 0 of the barrier, at most kStageSpin polls.
-__device__ __forceinline__ bool mbar_wait_bounded(const uint64_t *bar)
+// Wait for phase 0 of the barrier, at most `polls` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(const uint64_t *bar, long long polls)
 {
-  for (long long i = 0; i < kStageSpin; ++i) {
+  for (long long i = 0; i < polls; ++i) {
     if (mbar_try_wait(bar, 0)) return true;
     if (i > 64) __nanosleep(64);
   }
@@ -122,7 +123,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(const uint64_t *bar)
 __global__ void __launch_bounds__(256)
 brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny, int nz, int nbx,
                     int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range,
-                    int *__restrict__ timed_out)
+                    int *__restrict__ timed_out, long long first_polls)
 {
   __shared__ __align__(16) float rows[kRows * kRowSlot];
   __shared__ int lead[kRows];
@@ -171,7 +172,7 @@ brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny
   if (threadIdx.x == 0)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
   __syncthreads();
-  bool ok = mbar_wait_bounded(&bar);
+  bool ok = mbar_wait_bounded(&bar, first_polls);
   // rows that could not be copied in bulk: plain loads
   for (int r = 0; r < kRows; ++r) {
     if (!plain[r]) continue;
@@ -182,8 +183,13 @@ brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny
   }
   if (!ok) {
     atomicOr(timed_out, 1);
-    // the copies may still land in shared memory: wait for them once more
-    mbar_wait_bounded(&bar);
+    // The copies may still land in shared memory: wait for them once more,
+    // for the full bound. If this wait gives up too, the block goes on and
+    // exits while copies may still be landing in its shared memory; the
+    // bricks it writes are marked non-finite either way, and the host reports
+    // GVR_ERR_TIMEOUT. Only a copy that takes longer than both bounds
+    // together (seconds) reaches that case.
+    mbar_wait_bounded(&bar, kStageSpin);
   }
   __syncthreads();
   // warp w writes bricks run * 16 + w and run * 16 + 8 + w
@@ -220,6 +226,22 @@ brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny
 
 namespace {
 
+// Poll limit of the staged kernel's first wait for its bulk copies:
+// kStageSpin, or GVR_STAGE_WAIT_POLLS from the environment (0 .. kStageSpin),
+// read at every launch. Setting it to 0 makes every first wait give up at
+// once, which exercises the timeout path (flag, non-finite ranges,
+// GVR_ERR_TIMEOUT) while the second, full-length wait still lets the copies
+// land before the block exits.
+long long stage_first_polls()
+{
+  const char *v = getenv("GVR_STAGE_WAIT_POLLS");
+  if (!v || !*v) return kStageSpin;
+  char *end = nullptr;
+  const long long n = strtoll(v, &end, 10);
+  if (end == v || n < 0) return kStageSpin;
+  return n < kStageSpin ? n : kStageSpin;
+}
+
 // Brick a field in device memory: the staged kernel for contiguous float32,
 // the per-brick gather otherwise.
 cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int dims[3],
@@ -233,7 +255,7 @@ cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int
               (unsigned)nbrick[2]);
     brick_staged_kernel<<<grid, 256, 0, stream>>>((const float *)dsrc, n, dims[0], dims[1], dims[2],
                                                   nbrick[0], nbrick[1], d_bricks, d_brick_range,
-                                                  d_timed_out);
+                                                  d_timed_out, stage_first_polls());
   } else {
     brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1], dims[2],
                                                    nbrick[0], nbrick[1], d_bricks, d_brick_range);

@@ -260,7 +260,15 @@ GVR_API int gvr_scene_update_field(gvr_scene *scene, int domain_id, const void *
  * domain, 8 at most, about 1 GB in all) while earlier domains are bricked
  * on `stream`; ranges are reduced on the device and read back once. Host
  * fields in pinned memory overlap best. Returns after the uploads are
- * complete. */
+ * complete.
+ *
+ * Contiguous float32 fields are bricked from shared memory filled by bulk
+ * async copies, which the kernel waits for with a bounded wait. If that wait
+ * gives up, the bricks are written with non-finite ranges, the call (and
+ * gvr_scene_update_field / the add calls) returns GVR_ERR_TIMEOUT, and the
+ * domains' ranges stay NaN until the fields are published again. The
+ * environment variable GVR_STAGE_WAIT_POLLS (0 .. 4194304, default the
+ * maximum) sets the first wait's poll limit; 0 exercises that path. */
 GVR_API int gvr_scene_update_fields(gvr_scene *scene, int n, const int *domain_ids,
                                     const void *const *fields, int dtype, int64_t stride,
                                     int location, void *stream);
@@ -281,7 +289,8 @@ GVR_API int gvr_scene_set_tuning(gvr_scene *scene, int packet_w, int unroll,
 GVR_API int gvr_scene_bounds(const gvr_scene *scene, int domain_id, double bounds[6]);
 
 /* Global scalar range {min,max} of the scene field (Renderer::PreExecute,
- * Renderer.cpp:144-179). */
+ * Renderer.cpp:144-179). Both NaN while a domain's last field publish
+ * returned GVR_ERR_TIMEOUT (publish the field again). */
 GVR_API int gvr_scene_range(const gvr_scene *scene, double range[2]);
 
 /* ------------------------------------------------------------------ */
@@ -428,6 +437,40 @@ GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_p
  * stream-ordered on `stream`. */
 GVR_API int gvr_canvas_to_rgba8(const float *rgba, int width, int height, uint8_t *out,
                                 int location, void *stream);
+
+/* Z-buffer compositing of n_images opaque canvases of width x height
+ * pixels (RGBA float, row-major, + depth float): Renderer::Composite in
+ * Z_BUFFER_SURFACE mode, which composites the per-domain (or per-plot)
+ * renders of the opaque plots before the volume pass draws over them
+ * (vtkh/rendering/Renderer.cpp:111-142; Compositor::AddImage,
+ * vtkh/compositing/Compositor.cpp:86-125; ImageCompositor::ZBufferComposite,
+ * ImageCompositor.hpp:49-76). Each canvas goes through the 8-bit vtkh::Image
+ * (channel = (unsigned char)(value * 255), depth = |depth|, Image.hpp:80-113);
+ * image 0 is kept, and image k > 0 replaces a pixel where its depth is <= 1
+ * and not behind the kept depth; the result comes back as value / 255 with
+ * the kept depth (Renderer::ImageToCanvas, Renderer.cpp:271-289). The output
+ * is what gvr_render_volume_over takes as its opaque canvas (Scene.cpp:
+ * 154-212). rgba[k] / depth[k] point at the canvases (4 W H and W H floats),
+ * all on the side `location` names; n_images 1 .. 64. With GVR_MEM_HOST the
+ * call stages the canvases through pooled scratch and returns when the output
+ * is written; with GVR_MEM_DEVICE it is stream-ordered on `stream`. */
+GVR_API int gvr_zbuffer_composite(int n_images, const float *const *rgba,
+                                  const float *const *depth, int width, int height,
+                                  float *out_rgba, float *out_depth, int location, void *stream);
+
+/* Give the library's scratch memory on `device` back to the system down to
+ * keep_bytes (0: everything not in use); no counterpart in the reference.
+ * The partial compositor, the adjoint and the device PNG conversion take
+ * their scratch from a stream-ordered pool of this library that keeps its
+ * blocks between calls (its footprint grows to the largest call's scratch
+ * and stays reserved until the process exits or this call trims it), so
+ * that repeated calls neither map fresh pages nor synchronise. An in-situ
+ * host that needs the memory back between visualisation steps calls this;
+ * the next call that needs scratch allocates it again. reserved_out (may be
+ * NULL) receives the bytes the pool still reserves. Synchronise the streams
+ * that used the library before trimming, or their last frees may not have
+ * completed yet. */
+GVR_API int gvr_scratch_trim(int device, uint64_t keep_bytes, uint64_t *reserved_out);
 
 /* Render one uniform domain without allocating any device memory; no
  * counterpart in the reference. For callers that may not call cudaMalloc or

@@ -287,6 +287,48 @@ int or_visibility_order(const gvr_camera *c, const double *bounds, int n,
 }
 
 /* ------------------------------------------------------------------ */
+/* Z-buffer compositing of opaque canvases                              */
+/* ------------------------------------------------------------------ */
+
+/* Image::Init (vtkh/compositing/Image.hpp:80-113): 8-bit colour by a
+ * truncating cast of value * 255 (float arithmetic), depth made positive. */
+static unsigned char or_u8(float v)
+{
+  float s = v * 255.f;
+  if (s < 0.f) s = 0.f;
+  if (s > 255.f) s = 255.f;
+  return (unsigned char)s;
+}
+
+/* Renderer::Composite in Z_BUFFER_SURFACE mode for n canvases (Renderer.cpp:
+ * 111-142): the first canvas is kept (Compositor::AddImage, Compositor.cpp:
+ * 86-125), each later one composited into it by ImageCompositor::
+ * ZBufferComposite (ImageCompositor.hpp:49-76: skip where its depth > 1 or
+ * the kept depth is nearer, else take its pixel and |depth|), and the result
+ * converted back by Renderer::ImageToCanvas (Renderer.cpp:271-289). */
+int or_zbuffer_composite(int n, const float *const *rgba, const float *const *depth,
+                         int width, int height, float *out_rgba, float *out_depth)
+{
+  if (n < 1 || width < 1 || height < 1) return GVR_ERR_INVALID_ARGUMENT;
+  const long long size = (long long)width * height;
+  for (long long i = 0; i < size; ++i) {
+    unsigned char px[4];
+    for (int c = 0; c < 4; ++c) px[c] = or_u8(rgba[0][4 * i + c]);
+    float d = depth[0][i] < 0.f ? -depth[0][i] : depth[0][i];
+    for (int k = 1; k < n; ++k) {
+      float dk = depth[k][i] < 0.f ? -depth[k][i] : depth[k][i];
+      if (dk > 1.f || d < dk) continue;
+      d = dk;
+      for (int c = 0; c < 4; ++c) px[c] = or_u8(rgba[k][4 * i + c]);
+    }
+    const float one_over_255 = 1.f / 255.f;
+    for (int c = 0; c < 4; ++c) out_rgba[4 * i + c] = (float)px[c] * one_over_255;
+    out_depth[i] = d;
+  }
+  return GVR_OK;
+}
+
+/* ------------------------------------------------------------------ */
 /* Partial compositing (PartialCompositor::composite_partials and       */
 /* BlendPartials, VolumePartial::blend)                                 */
 /* ------------------------------------------------------------------ */

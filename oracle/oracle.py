@@ -106,6 +106,7 @@ def load(precision: int = 64) -> C.CDLL:
     lib.or_cinema_cameras.argtypes = [P(d), P(f), i, vp]
     lib.or_visibility_order.argtypes = [vp, P(d), i, P(i)]
     lib.or_composite_partials.argtypes = [i, P(i), vp, vp]
+    lib.or_zbuffer_composite.argtypes = [i, P(vp), P(vp), i, i, P(f), P(f)]
     lib.or_scene_new.restype = vp
     lib.or_scene_free.argtypes = [vp]
     lib.or_scene_add_uniform.argtypes = [vp, P(i), P(d), P(d), P(f), i]
@@ -249,6 +250,22 @@ def composite_partials(images, precision: int = 64, reference: bool = False) -> 
         n = load(precision).or_composite_partials(len(images), counts_p, flat.ctypes.data,
                                                   out.ctypes.data)
     return out[:n].copy()
+
+
+def zbuffer_composite(rgba_images, depth_images):
+    """Renderer::Composite in Z_BUFFER_SURFACE mode (or_zbuffer_composite):
+    lists of (H, W, 4) / (H, W) float arrays -> the composited canvas."""
+    cols = [np.ascontiguousarray(c, dtype=np.float32) for c in rgba_images]
+    deps = [np.ascontiguousarray(d, dtype=np.float32) for d in depth_images]
+    h, w = cols[0].shape[:2]
+    out = np.zeros((h, w, 4), np.float32)
+    out_d = np.zeros((h, w), np.float32)
+    cp = (C.c_void_p * len(cols))(*[c.ctypes.data for c in cols])
+    dp = (C.c_void_p * len(deps))(*[d.ctypes.data for d in deps])
+    rc = load(64).or_zbuffer_composite(len(cols), cp, dp, w, h, fptr(out), fptr(out_d))
+    if rc != 0:
+        raise RuntimeError(f"oracle z-buffer composite failed with status {rc}")
+    return out, out_d
 
 
 def composite_partials_f32(images) -> np.ndarray:

@@ -149,3 +149,11 @@ def test_device_png_conversion_wants_a_cuda_tensor():
     from ascent_gb300 import png as PNG
     with pytest.raises(ValueError):
         PNG.canvas_to_rgba8_device(torch.zeros((2, 2, 4), dtype=torch.float32))
+
+
+def test_scratch_trim_arguments():
+    """gvr_scratch_trim needs no GPU for its argument checks; a device the
+    library never used holds no pool (0 bytes reserved)."""
+    with pytest.raises(N.GvrError):
+        N.scratch_trim(-1, 0)
+    assert N.scratch_trim(63, 0) == 0

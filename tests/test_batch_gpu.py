@@ -124,3 +124,27 @@ def test_batch_with_hex_and_uniform_domains():
     for v, cam in enumerate(cams):
         assert_parity(rgba[v], osc.render(cam, p)[0])
     assert rgba[..., 3].max() > 0.1
+
+
+def test_cinema_shaped_batch_matches_oracle():
+    """The batched configuration's shape: 37 uniform domains of uneven sizes
+    (edges from {32, ..., 256} cells, seeded splits of a 256^3 box) and a
+    4 x 2 Cinema sweep, against the FP64 oracle with the oracle's own
+    cameras and parameters, at 128^2."""
+    wl = W.cinema_batch(width=128, height=128, n_phi=4, n_theta=2)
+    assert len(wl.domains) == 37
+    assert len({d.dims for d in wl.domains}) > 5  # uneven
+    cams = S.cinema_cameras(wl.bounds, wl.phi_theta)
+    p = V.workload_params(wl)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        rgba, _ = sc.render_batch(cams, p)
+    osc = O.OracleScene(64)
+    for d in wl.domains:
+        osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    ocams = O.cinema_cameras(wl.bounds, wl.phi_theta)
+    op = O.workload_params(wl)
+    for v in range(len(cams)):
+        o, _, _ = osc.render(ocams[v], op)
+        assert o[..., 3].max() > 0.1
+        assert_parity(rgba[v], o)

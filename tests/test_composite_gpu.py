@@ -101,3 +101,21 @@ def test_sparse_pixel_ids_take_the_sorting_path(comp):
     a["rgb"] = (rng.uniform(0, 1, (6000, 3)) * a["alpha"][:, None]).astype(np.float32)
     ims = [a[:2500], a[2500:]]
     assert comp.PartialCompositor().composite(ims).tobytes() == O.composite_partials_f32(ims).tobytes()
+
+
+def test_scratch_trim_returns_pooled_memory(comp):
+    """The compositor's scratch stays in the library's pool between calls;
+    gvr_scratch_trim gives it back, and the next call allocates it again
+    with the same result."""
+    import torch
+    from ascent_gb300 import _native as N
+    rng = np.random.default_rng(21)
+    ims = _random_partials(rng, 4, density=0.7)
+    first = comp.PartialCompositor().composite(ims)
+    torch.cuda.synchronize()
+    held = N.scratch_trim(0, 1 << 62)   # keep everything: reports the pool size
+    assert held > 0
+    assert N.scratch_trim(0, 0) == 0
+    again = comp.PartialCompositor().composite(ims)
+    assert again.tobytes() == first.tobytes()
+    assert N.scratch_trim(0, 1 << 62) > 0

@@ -5,8 +5,11 @@ synchronise the device under the simulation's streams).
 
 It is called here through the C ABI with caller-owned device buffers, twice
 in a row, and each result is checked against gvr_render_volume on a scene
-holding the same single domain, with the parity bar the other GPU tests use.
-This file is named to be collected last.
+holding the same single domain and against the FP64 oracle (set up by its
+own functions), with the parity bar the other GPU tests use. The device's
+free memory after the second call must equal its free memory after the
+first (the first call on a device may load the library's kernels). This
+file is named to be collected last.
 """
 import ctypes as C
 
@@ -17,6 +20,7 @@ from ascent_gb300 import _native as N
 from ascent_gb300 import scene as S
 from ascent_gb300 import volume as V
 from ascent_gb300 import workloads as W
+from oracle import oracle as O
 
 from conftest import assert_parity
 
@@ -49,22 +53,30 @@ def test_noalloc_matches_scene_render_on_two_calls_in_a_row():
     origin = (C.c_double * 3)(*d.origin)
     spacing = (C.c_double * 3)(*d.spacing)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    osc = O.OracleScene(64)
+    osc.add_uniform(d.dims, d.origin, d.spacing, d.field)
+    oracle_img, _, _ = osc.render(O.workload_camera(wl), O.workload_params(wl))
     fn = noalloc_fn()
     outs = []
+    free_after = []
     for _ in range(2):
         rgba.fill_(-1.0)
+        torch.cuda.synchronize()
         n = C.c_uint64(0)
         rc = fn(C.c_void_p(field.data_ptr()), dims, origin, spacing, C.byref(cam), C.byref(p),
                 C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()), stream, C.byref(n))
         assert rc == 0, N.lib().gvr_last_error()
         torch.cuda.synchronize()
+        free_after.append(torch.cuda.mem_get_info()[0])
         g = rgba.cpu().numpy()
         gd = depth.cpu().numpy()
         assert_parity(g, ref)
+        assert_parity(g, oracle_img)
         np.testing.assert_allclose(gd, ref_depth, rtol=0, atol=1e-5)
         assert n.value == ref_n
         outs.append(g)
     np.testing.assert_array_equal(outs[0], outs[1])
+    assert free_after[1] == free_after[0], free_after
     assert ref[..., 3].max() > 0.2
 
 
