@@ -64,6 +64,27 @@ def composite_partials_device(partials, stream=None):
     return out[:n_out.value]
 
 
+def composite_partials_device_async(partials, pixel_lo: int, pixel_hi: int, out=None, n_out=None,
+                                    stream=None):
+    """Composite device partials whose pixel ids lie in [pixel_lo, pixel_hi]
+    with no host synchronisation (gvr_composite_partials_async). Returns
+    (out, n_out): an (n, 6) int32 tensor of which the first n_out rows are
+    the result, and n_out as a one-element int64 CUDA tensor (-1 if a record
+    was outside the range). Reading n_out waits for the work."""
+    import torch
+    if partials.dtype != torch.int32 or partials.dim() != 2 or partials.shape[1] != 6 or not partials.is_cuda:
+        raise N.GvrError(N.GVR_ERR_INVALID_ARGUMENT, "device partials must be an (n, 6) int32 CUDA tensor")
+    parts = partials.contiguous()
+    if out is None:
+        out = torch.empty_like(parts)
+    if n_out is None:
+        n_out = torch.zeros(1, dtype=torch.int64, device=parts.device)
+    n = parts.shape[0]
+    N.call("gvr_composite_partials_async", parts.data_ptr() if n else None, n, int(pixel_lo), int(pixel_hi),
+           out.data_ptr() if n else None, n_out.data_ptr(), C.c_void_p(_stream_ptr(stream)))
+    return out, n_out
+
+
 def to_device(partials: np.ndarray, device="cuda"):
     import torch
     raw = np.ascontiguousarray(partials, dtype=PARTIAL_DTYPE).view(np.int32).reshape(-1, 6)

@@ -147,22 +147,42 @@ __global__ void range_kernel(const Partial *__restrict__ in, int64_t n, unsigned
 }
 
 // cnt[p] = records of pixel lo + p; rank[i] = record i's slot in its bucket
-// (in arrival order; the emit kernel restores input order).
-__global__ void count_kernel(const Partial *__restrict__ in, int64_t n, int lo,
-                             uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank)
+// (in arrival order; the emit kernel restores input order). A record whose
+// id lies outside [lo, lo + r) (possible only when the caller gave the
+// range) is left out and sets *bad.
+__global__ void count_kernel(const Partial *__restrict__ in, int64_t n, int lo, int64_t r,
+                             uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank,
+                             unsigned *__restrict__ bad)
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    rank[i] = atomicAdd(cnt + (in[i].pixel_id - lo), 1u);
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = (int64_t)in[i].pixel_id - lo;
+    if (p < 0 || p >= r) {
+      atomicOr(bad, 1u);
+      continue;
+    }
+    rank[i] = atomicAdd(cnt + p, 1u);
+  }
 }
 
-__global__ void bucket_kernel(const Partial *__restrict__ in, int64_t n, int lo,
+__global__ void bucket_kernel(const Partial *__restrict__ in, int64_t n, int lo, int64_t r,
                               const uint32_t *__restrict__ off, const uint32_t *__restrict__ rank,
                               uint32_t *__restrict__ order)
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    order[off[in[i].pixel_id - lo] + rank[i]] = (uint32_t)i;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = (int64_t)in[i].pixel_id - lo;
+    if (p < 0 || p >= r) continue;
+    order[off[p] + rank[i]] = (uint32_t)i;
+  }
+}
+
+// Output count of the caller-range path into the caller's device int64:
+// -1 when a record's pixel id was outside the given range.
+__global__ void count_out_kernel(const uint32_t *__restrict__ totals, const unsigned *__restrict__ bad,
+                                 int64_t *__restrict__ n_out)
+{
+  if (threadIdx.x == 0) *n_out = *bad ? -1 : (int64_t)totals[0] + totals[1];
 }
 
 // upos[p] = 1 for pixels with one record, mpos[p] = 1 for pixels with more
@@ -265,7 +285,7 @@ struct Arena {
 
 size_t dense_bytes(int64_t n, int64_t r)
 {
-  return 256 * 8 + (4 * (size_t)r + 2 * (size_t)n + scan_scratch_words(r) + 2) * sizeof(uint32_t);
+  return 256 * 9 + (4 * (size_t)r + 2 * (size_t)n + scan_scratch_words(r) + 3) * sizeof(uint32_t);
 }
 
 size_t sorted_bytes(int64_t n)
@@ -276,7 +296,7 @@ size_t sorted_bytes(int64_t n)
 
 // Dense pixel ids: histogram, bucket, per-pixel emit.
 cudaError_t composite_dense(const Partial *in, int64_t n, int lo, int64_t r, Partial *out,
-                            Arena &a, uint32_t *totals, cudaStream_t st)
+                            Arena &a, uint32_t *totals, unsigned *bad, cudaStream_t st)
 {
   uint32_t *cnt = a.take<uint32_t>(r), *off = a.take<uint32_t>(r);
   uint32_t *upos = a.take<uint32_t>(r), *mpos = a.take<uint32_t>(r);
@@ -284,11 +304,11 @@ cudaError_t composite_dense(const Partial *in, int64_t n, int lo, int64_t r, Par
   uint32_t *scan_tmp = a.take<uint32_t>(scan_scratch_words(r));
   cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * r, st);
   if (e != cudaSuccess) return e;
-  count_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, cnt, rank);
+  count_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, cnt, rank, bad);
   count_launch();
   if ((e = cudaMemcpyAsync(off, cnt, sizeof(uint32_t) * r, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
   if ((e = exclusive_scan(off, r, scan_tmp, st)) != cudaSuccess) return e;
-  bucket_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, off, rank, order);
+  bucket_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, off, rank, order);
   count_launch();
   pixel_flag_kernel<<<grid_of(r), 256, 0, st>>>(cnt, r, upos, mpos);
   count_launch();
@@ -378,7 +398,9 @@ extern "C" int gvr_composite_partials(const gvr_partial *partials, int64_t n, gv
     const size_t bytes = dense ? dense_bytes(n, r) : sorted_bytes(n);
     CP_TRY(scratch_alloc((void **)&arena.base, bytes, st), "allocate scratch");
     totals = arena.take<uint32_t>(2);
-    CP_TRY(dense ? composite_dense(d_in, n, lo, r, d_out, arena, totals, st)
+    // the range was measured, so no record is outside it: mm[0] serves as
+    // the (unused) flag word
+    CP_TRY(dense ? composite_dense(d_in, n, lo, r, d_out, arena, totals, mm, st)
                  : composite_sorted(d_in, n, d_out, arena, totals, st),
            "composite");
     CP_TRY(cudaMemcpyAsync(ht, totals, sizeof(ht), cudaMemcpyDeviceToHost, st), "read counts");
@@ -399,4 +421,39 @@ done:
   if (mm) cudaFreeAsync(mm, st);
   if (arena.base) cudaFreeAsync(arena.base, st);
   return rc;
+}
+
+extern "C" int gvr_composite_partials_async(const gvr_partial *partials, int64_t n, int32_t pixel_lo,
+                                            int32_t pixel_hi, gvr_partial *out, int64_t *n_out,
+                                            void *stream)
+{
+  if (!n_out || n < 0 || (n > 0 && (!partials || !out)))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad partial arrays");
+  if (pixel_hi < pixel_lo) return set_error(GVR_ERR_INVALID_ARGUMENT, "pixel_hi < pixel_lo");
+  if (n >= ((int64_t)1 << 31)) return set_error(GVR_ERR_UNSUPPORTED, "at most 2^31 - 1 partials");
+  const int64_t r = (int64_t)pixel_hi - pixel_lo + 1;
+  if (r > ((int64_t)1 << 30)) return set_error(GVR_ERR_UNSUPPORTED, "pixel range above 2^30");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (n == 0) {
+    e = cudaMemsetAsync(n_out, 0, sizeof(int64_t), st);
+    return e == cudaSuccess ? GVR_OK : cuda_error(e, "composite");
+  }
+  Arena arena;
+  e = scratch_alloc((void **)&arena.base, dense_bytes(n, r), st);
+  if (e != cudaSuccess) return cuda_error(e, "allocate scratch");
+  uint32_t *totals = arena.take<uint32_t>(2);
+  unsigned *bad = arena.take<unsigned>(1);
+  e = cudaMemsetAsync(bad, 0, sizeof(unsigned), st);
+  if (e == cudaSuccess)
+    e = composite_dense(reinterpret_cast<const Partial *>(partials), n, pixel_lo, r,
+                        reinterpret_cast<Partial *>(out), arena, totals, bad, st);
+  if (e == cudaSuccess) {
+    count_out_kernel<<<1, 32, 0, st>>>(totals, bad, n_out);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(arena.base, st);
+  if (e != cudaSuccess) return cuda_error(e, "composite");
+  return GVR_OK;
 }

@@ -33,6 +33,14 @@ constexpr int kHexNewtonSteps = 10;        // NewtonSolve default_max_steps
 // test allows 2e-4: tighter bounds leave samples near faces unlocated in
 // every neighbouring cell.
 constexpr float kHexNewtonTol = 2e-3f;     // |step|_inf in reference space
+// From the guess extrapolated along a ray the first step is ~0.02 and
+// already leaves an error of ~1e-4 (a CPU emulation of the solve on a
+// jittered mesh: 4.9e-5 median, 6.4e-4 p99), so a step below 0.05 is also
+// accepted when the solution lies at least kHexLooseMargin inside every
+// face; near a face, where such an error could decide which cell holds the
+// sample, the solve goes on to kHexNewtonTol.
+constexpr float kHexLooseTol = 0.05f;
+constexpr float kHexLooseMargin = 0.01f;
 constexpr float kHexInsideTol = 2e-4f;     // r, s, t in [-tol, 1 + tol]
 constexpr int kHexStack = 64;
 constexpr int kHexHops = 4;                // face-neighbour steps before the LBVH walk
@@ -67,10 +75,12 @@ __device__ __forceinline__ float hex_value(const float4 (&c)[8], float r, float 
 // the reference coordinates of p, outside [0,1]^3), -1 when it failed.
 // When it converged and `step` is given, drst receives J^-1 step with the
 // last Jacobian: the change of rst over a world-space displacement `step`
-// (the next sample's guess along a ray).
+// (the next sample's guess along a ray). `loose` allows the kHexLooseTol
+// acceptance away from faces (the march's solves from an extrapolated
+// guess; point location from the cell centre keeps the tight rule).
 __device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const float p[3],
                                                  float rst[3], const float *step = nullptr,
-                                                 float *drst = nullptr)
+                                                 float *drst = nullptr, bool loose = false)
 {
   float r = rst[0], s = rst[1], t = rst[2];
   bool conv = false;
@@ -109,7 +119,10 @@ __device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const flo
     s -= d1;
     t -= d2;
     if (!(fabsf(r) < 1e3f && fabsf(s) < 1e3f && fabsf(t) < 1e3f)) return -1;
-    if (fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2))) < kHexNewtonTol) {
+    const float dmax = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+    const bool deep = loose && fminf(fminf(r, s), t) > kHexLooseMargin &&
+                      fmaxf(fmaxf(r, s), t) < 1.f - kHexLooseMargin;
+    if (dmax < kHexNewtonTol || (dmax < kHexLooseTol && deep)) {
       conv = true;
       if (step) {
         drst[0] = (c00 * step[0] + c10 * step[1] + c20 * step[2]) * id;

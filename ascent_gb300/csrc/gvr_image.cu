@@ -96,7 +96,9 @@ extern "C" int gvr_zbuffer_composite(int n_images, const float *const *rgba,
   if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
     return set_error(GVR_ERR_INVALID_ARGUMENT, "bad location");
   const int64_t pixels = (int64_t)width * height;
-  const size_t per = (size_t)pixels * (sizeof(float4) + sizeof(float));
+  // one canvas per block: colour (16-byte aligned) then depth; blocks padded
+  // to 256 bytes so that every colour array stays float4-aligned
+  const size_t per = ((size_t)pixels * (sizeof(float4) + sizeof(float)) + 255) & ~(size_t)255;
   cudaStream_t st = (cudaStream_t)stream;
   ZImages im{};
   float4 *d_out = reinterpret_cast<float4 *>(out_rgba);

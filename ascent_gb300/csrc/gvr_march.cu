@@ -28,6 +28,11 @@ namespace {
 
 constexpr int kTile = kMarchTile;  // CTA tile edge in pixels
 constexpr int kThreads = 256; // 8 warps, each a 32-ray packet
+// Per-ray compositing state kept in shared memory while a domain is marched
+// (rgb, front depth, last entry distance, covered exit, last domain, ray
+// end, pixel): parked there rather than in registers, the unrolled march
+// loop fits 64 registers (4 CTAs per SM) with little or no spilling.
+constexpr int kStateSlots = 10;
 
 struct Ray {
   float o[3];
@@ -85,7 +90,7 @@ __device__ __forceinline__ int rect_cell(const float *__restrict__ x, int n, flo
 
 // March one structured domain over [t0, t1): accumulates the domain's
 // partial in acc and returns the number of samples the stepping rule takes.
-__device__ int march_domain(const DomainDev &dm, const Ray &r, float t0, float t1,
+__device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, float t0, float t1,
                             const MarchParams &mp, const float4 *lut, float thr,
                             float4 &acc)
 {
@@ -440,7 +445,7 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
           g[face >> 1] += (face & 1) ? -1.f : 1.f;
         }
       }
-      int st = hex_newton_status(v, p, g, step, drst);
+      int st = hex_newton_status(v, p, g, step, drst, true);
       // left the cell: step to the neighbour across the face it left
       // through (Newton's outside solution names it), a few times at most
       for (int hop = 0; st == 0 && hop < kHexHops && dm.hex_nbr; ++hop) {
@@ -454,7 +459,7 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
         g[0] = __saturatef(g[0]);
         g[1] = __saturatef(g[1]);
         g[2] = __saturatef(g[2]);
-        st = hex_newton_status(v, p, g, step, drst);
+        st = hex_newton_status(v, p, g, step, drst, true);
       }
       if (st == 1) {
         found = true;
@@ -488,10 +493,13 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
 // Everything one ray does: march the candidate domains (bits of `mask`) in
 // increasing exit distance, blend their partials, and finish the pixel
 // (image depth, uint8 round trip, background). Returns the samples taken.
+// g_state: the CTA's shared-memory slots for the state that must survive
+// the march of a domain (kStateSlots words per thread, slot k of thread i
+// at g_state[k * kThreads + i]).
 template <int UNROLL, bool HEX>
 __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, const ViewDev &view,
                                           const MarchParams &mp, const float4 *lut, int px, int py,
-                                          float4 &out, float &dep)
+                                          float4 &out, float &dep, float *g_state)
 {
   int count = 0;
   Ray r;
@@ -513,12 +521,10 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
   // Opaque canvas: the ray ends at the world point of the canvas depth
   // (MapCanvasToRays: pixel (i, j) at depth d unprojected from NDC
   // (2i/W - 1, 2j/H - 1, 2d - 1); FP64, as in the oracle).
-  float4 cin = make_float4(0.f, 0.f, 0.f, 0.f);
-  float din = mp.clear_depth, t_max = FLT_MAX;
+  float t_max = FLT_MAX;
   if (mp.canvas_depth) {
     const int64_t pix = (int64_t)py * mp.width + px;
-    cin = mp.canvas_rgba[pix];
-    din = mp.canvas_depth[pix];
+    const float din = mp.canvas_depth[pix];
     const double xn = 2.0 * px / mp.width - 1.0, yn = 2.0 * py / mp.height - 1.0;
     const double zn = 2.0 * (double)din - 1.0;
     const double *I = view.inv_projview;
@@ -532,10 +538,22 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     }
   }
 
-  float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f;
+  // Compositing state that lives across the march of a domain is parked in
+  // shared memory (one word per thread per slot, st[k * kThreads]), so the
+  // march loop gets the registers.
+  float *st = g_state + threadIdx.x;
+  st[7 * kThreads] = t_max;
+  st[8 * kThreads] = __int_as_float(px);
+  st[9 * kThreads] = __int_as_float(py);
+  st[0 * kThreads] = 0.f;          // composited rgb
+  st[1 * kThreads] = 0.f;
+  st[2 * kThreads] = 0.f;
+  st[3 * kThreads] = 0.f;          // depth of the front partial
+  st[4 * kThreads] = -FLT_MAX;     // entry distance of the last domain
+  st[5 * kThreads] = -FLT_MAX;     // furthest exit covered
+  st[6 * kThreads] = __int_as_float(-1);  // last domain
+  float ca = 0.f;
   bool have = false;
-  float last_t0 = -FLT_MAX, covered = -FLT_MAX;
-  int last_d = -1;
   for (;;) {
     if (ca >= mp.early_term) break;
     // Next domain along the ray by (entry distance, index). Domains tile
@@ -546,20 +564,27 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     // (pixel, depth = exit distance) sort.
     int best = -1;
     float bt0 = FLT_MAX, bt1 = 0.f;
-    for (uint64_t m = mask; m; m &= m - 1) {
-      const int dd = __ffsll((long long)m) - 1;
-      float t0, t1;
-      if (!slab(doms[dd], r, t0, t1)) continue;
-      const bool after = t0 > last_t0 || (t0 == last_t0 && dd > last_d);
-      const bool before = best < 0 || t0 < bt0;
-      if (after && before) { best = dd; bt0 = t0; bt1 = t1; }
+    {
+      const float last_t0 = st[4 * kThreads];
+      const int last_d = __float_as_int(st[6 * kThreads]);
+      for (uint64_t m = mask; m; m &= m - 1) {
+        const int dd = __ffsll((long long)m) - 1;
+        float t0, t1;
+        if (!slab(doms[dd], r, t0, t1)) continue;
+        const bool after = t0 > last_t0 || (t0 == last_t0 && dd > last_d);
+        const bool before = best < 0 || t0 < bt0;
+        if (after && before) { best = dd; bt0 = t0; bt1 = t1; }
+      }
     }
     if (best < 0) break;
-    last_t0 = bt0;
-    last_d = best;
-    bt0 = fmaxf(bt0, covered);
-    bt1 = fminf(bt1, t_max);
-    covered = fmaxf(covered, bt1);
+    st[4 * kThreads] = bt0;
+    st[6 * kThreads] = __int_as_float(best);
+    {
+      const float covered = st[5 * kThreads];
+      bt0 = fmaxf(bt0, covered);
+      bt1 = fminf(bt1, st[7 * kThreads]);
+      st[5 * kThreads] = fmaxf(covered, bt1);
+    }
     const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const DomainDev &dm = doms[best];
@@ -574,19 +599,31 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
       count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
     if (acc.w < mp.alpha_cull) continue;
     if (!have) {
-      crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
-      cdepth = bt1;
+      st[0 * kThreads] = acc.x; st[1 * kThreads] = acc.y; st[2 * kThreads] = acc.z;
+      ca = acc.w;
+      st[3 * kThreads] = bt1;
       have = true;
     } else if (ca < 1.f && acc.w != 0.f) {
       const float op = 1.f - ca;
-      crgb[0] = fmaf(op, acc.x, crgb[0]);
-      crgb[1] = fmaf(op, acc.y, crgb[1]);
-      crgb[2] = fmaf(op, acc.z, crgb[2]);
+      st[0 * kThreads] = fmaf(op, acc.x, st[0 * kThreads]);
+      st[1 * kThreads] = fmaf(op, acc.y, st[1 * kThreads]);
+      st[2 * kThreads] = fmaf(op, acc.z, st[2 * kThreads]);
       ca = fminf(fmaf(op, acc.w, ca), 1.f);
     }
   }
+  const float crgb[3] = {st[0], st[kThreads], st[2 * kThreads]};
+  const float cdepth = st[3 * kThreads];
+  px = __float_as_int(st[8 * kThreads]);
+  py = __float_as_int(st[9 * kThreads]);
 
   // partials_to_canvas: the composited partial in front of the canvas
+  float4 cin = make_float4(0.f, 0.f, 0.f, 0.f);
+  float din = mp.clear_depth;
+  if (mp.canvas_depth) {
+    const int64_t pix = (int64_t)py * mp.width + px;
+    cin = mp.canvas_rgba[pix];
+    din = mp.canvas_depth[pix];
+  }
   out = cin;
   dep = din;
   if (have) {
@@ -642,6 +679,7 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
   const int tile = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
   const int tile_x = tile % tiles_x, tile_y = tile / tiles_x;
   extern __shared__ float4 smem[];
+  __shared__ float s_state[kStateSlots * kThreads];
   float4 *lut = smem;
   DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
   for (int i = threadIdx.x; i < mp.lut_size; i += kThreads) lut[i] = g_lut[i];
@@ -662,7 +700,7 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
     const uint64_t all = mp.n_domains >= 64 ? ~0ull : ((1ull << mp.n_domains) - 1ull);
     float4 out;
     float dep;
-    count = render_ray<UNROLL, HEX>(doms, all, view, mp, lut, px, py, out, dep);
+    count = render_ray<UNROLL, HEX>(doms, all, view, mp, lut, px, py, out, dep, s_state);
     const int64_t pix = (int64_t)py * mp.width + px;
     rgba[pix] = out;
     depth[pix] = dep;
@@ -698,6 +736,7 @@ batch_kernel(const DomainDev *__restrict__ g_domains, const ViewDev *__restrict_
   DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
   __shared__ unsigned int s_item;
   __shared__ unsigned int s_mask[2];
+  __shared__ float s_state[kStateSlots * kThreads];
   for (int i = threadIdx.x; i < mp.lut_size; i += kThreads) lut[i] = g_lut[i];
   {
     const int words = mp.n_domains * (int)(sizeof(DomainDev) / 4);
@@ -741,7 +780,7 @@ batch_kernel(const DomainDev *__restrict__ g_domains, const ViewDev *__restrict_
       if (px < mp.width && py < mp.height) {
         float4 out;
         float dep;
-        count += render_ray<UNROLL, HEX>(doms, mask, views[v], mp, lut, px, py, out, dep);
+        count += render_ray<UNROLL, HEX>(doms, mask, views[v], mp, lut, px, py, out, dep, s_state);
         const int64_t pix = (int64_t)v * pixels + (int64_t)py * mp.width + px;
         rgba[pix] = out;
         depth[pix] = dep;

@@ -518,7 +518,16 @@ def bench_composite(dev, n_images=8, size=1024, cover=0.8, reps=10) -> dict:
         out = CP.composite_partials_device(d)
     ms = _timed(lambda: CP.composite_partials_device(d), stream, reps)
     out = CP.from_device(CP.composite_partials_device(d))
-    exact = out.tobytes() == O.composite_partials_f32(ims).tobytes()
+    ref = O.composite_partials_f32(ims)
+    exact = out.tobytes() == ref.tobytes()
+    # the caller-range path: ids known to lie in [0, size^2), count left on
+    # the device, no host synchronisation inside the call
+    aout, an = CP.composite_partials_device_async(d, 0, size * size - 1)
+    for _ in range(3):
+        CP.composite_partials_device_async(d, 0, size * size - 1, out=aout, n_out=an)
+    async_ms = _timed(lambda: CP.composite_partials_device_async(d, 0, size * size - 1, out=aout, n_out=an),
+                      stream, reps)
+    async_exact = CP.from_device(aout[: int(an.item())]).tobytes() == ref.tobytes()
     t0 = time.perf_counter()
     O.composite_partials(ims, precision=32)
     cpu_s = time.perf_counter() - t0
@@ -527,6 +536,8 @@ def bench_composite(dev, n_images=8, size=1024, cover=0.8, reps=10) -> dict:
     return {"workload": f"composite{n_images}x{size}^2@{cover}", "records": len(flat),
             "pixels_out": len(out), "ms": ms, "grecords_per_s": len(flat) / ms / 1e6,
             "bit_identical_to_reference_order_f32": exact,
+            "caller_range_ms": async_ms, "caller_range_bit_identical": async_exact,
+            "caller_range_roofline_frac": alg / (async_ms / 1e3) / 1e9 / peaks()["hbm_gbs"],
             "cpu_oracle_ms": cpu_s * 1e3, "cpu_oracle_kind": "oracle C compositor (qsort, 1 thread)",
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": pk["hbm_gbs"],
                          "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / pk["hbm_gbs"],

@@ -438,6 +438,21 @@ GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_p
 GVR_API int gvr_canvas_to_rgba8(const float *rgba, int width, int height, uint8_t *out,
                                 int location, void *stream);
 
+/* gvr_composite_partials for device records whose pixel ids the caller
+ * bounds, without any host synchronisation; no counterpart in the
+ * reference (its composite is host code). Every record's pixel_id must lie
+ * in [pixel_lo, pixel_hi] — for partials of a W x H image, [0, W H - 1] —
+ * so the pixel-id range need not be measured and read back, and the output
+ * count is written to *n_out, a device int64, instead of being returned:
+ * the whole call is stream-ordered on `stream`. partials, out and n_out are
+ * device pointers; out needs room for n records. Same order and blend as
+ * gvr_composite_partials, bit for bit. A record outside the range is left
+ * out and *n_out becomes -1. Scratch: 16 bytes per pixel of the range plus
+ * 8 per record, from the library's pool. */
+GVR_API int gvr_composite_partials_async(const gvr_partial *partials, int64_t n,
+                                         int32_t pixel_lo, int32_t pixel_hi, gvr_partial *out,
+                                         int64_t *n_out, void *stream);
+
 /* Z-buffer compositing of n_images opaque canvases of width x height
  * pixels (RGBA float, row-major, + depth float): Renderer::Composite in
  * Z_BUFFER_SURFACE mode, which composites the per-domain (or per-plot)

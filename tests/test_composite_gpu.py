@@ -119,3 +119,31 @@ def test_scratch_trim_returns_pooled_memory(comp):
     again = comp.PartialCompositor().composite(ims)
     assert again.tobytes() == first.tobytes()
     assert N.scratch_trim(0, 1 << 62) > 0
+
+
+@pytest.mark.parametrize("seed,n_images,ties", [(30, 8, False), (31, 3, True), (32, 1, False)])
+def test_async_caller_range_bit_exact(comp, seed, n_images, ties):
+    """The caller-range path (no host synchronisation, device count) writes
+    the same records in the same order as the measured-range path."""
+    import torch
+    rng = np.random.default_rng(seed)
+    ims = _random_partials(rng, n_images, density=0.7, ties=ties)
+    flat = np.concatenate(ims)
+    lo, hi = int(flat["pixel_id"].min()) - 5, int(flat["pixel_id"].max()) + 7
+    d = comp.to_device(flat)
+    out, n_out = comp.composite_partials_device_async(d, lo, hi)
+    got = comp.from_device(out[: int(n_out.item())])
+    assert got.tobytes() == O.composite_partials_f32(ims).tobytes()
+
+
+def test_async_caller_range_flags_records_outside(comp):
+    import torch
+    rng = np.random.default_rng(33)
+    flat = np.concatenate(_random_partials(rng, 2, density=0.5))
+    d = comp.to_device(flat)
+    hi = int(flat["pixel_id"].max()) - 1   # the largest id lies outside
+    _, n_out = comp.composite_partials_device_async(d, int(flat["pixel_id"].min()), hi)
+    assert int(n_out.item()) == -1
+    empty = torch.zeros((0, 6), dtype=torch.int32, device="cuda")
+    _, n0 = comp.composite_partials_device_async(empty, 0, 10)
+    assert int(n0.item()) == 0
