@@ -496,7 +496,7 @@ static int upload_field(gvr_scene *s, Domain &d, const void *field, int dtype, i
   if (d.dev.assoc == GVR_ASSOC_VERTEX) {
     if (!s->d_flag && (e = cudaMalloc(&s->d_flag, sizeof(int))) != cudaSuccess)
       return cuda_error(e, "cudaMalloc flag");
-    e = launch_brick_field(field, dtype, stride, location == GVR_MEM_DEVICE, d.dev.dims,
+    e = launch_brick_field(field, dtype, stride, location == GVR_MEM_DEVICE, d.dev.dims, d.dev.bshift,
                            d.d_bricks, d.dev.nbrick, d.d_brick_range, d.range, d.stg, s->d_flag,
                            &timed_out, 0);
   } else {
@@ -536,9 +536,10 @@ static int add_structured(gvr_scene *s, int kind, const int dims[3], const doubl
   std::memset(&d.dev, 0, sizeof(d.dev));
   d.dev.kind = kind;
   d.dev.assoc = assoc;
+  d.dev.bshift = s->brick_shift;
   for (int a = 0; a < 3; ++a) {
     d.dev.dims[a] = dims[a];
-    d.dev.nbrick[a] = (dims[a] - 1 + kBrickCells - 1) / kBrickCells;
+    d.dev.nbrick[a] = (dims[a] - 1 + brick_cells(s->brick_shift) - 1) / brick_cells(s->brick_shift);
   }
   if (kind == GVR_DOMAIN_UNIFORM) {
     for (int a = 0; a < 3; ++a) {
@@ -577,13 +578,13 @@ static int add_structured(gvr_scene *s, int kind, const int dims[3], const doubl
   if (assoc == GVR_ASSOC_VERTEX) {
     d.n_values = (size_t)dims[0] * dims[1] * dims[2];
     d.n_bricks = (int64_t)d.dev.nbrick[0] * d.dev.nbrick[1] * d.dev.nbrick[2];
-    if (d.n_bricks * kBrickFloats >= (int64_t)1 << 31) {
+    if (d.n_bricks * brick_floats(d.dev.bshift) >= (int64_t)1 << 31) {
       free_domain(d);
       return set_error(GVR_ERR_UNSUPPORTED,
                        "a domain's bricked field must hold < 2^31 floats (about 1290^3 nodes); "
                        "split it into more domains");
     }
-    e = cudaMalloc(&d.d_bricks, sizeof(float) * kBrickFloats * d.n_bricks);
+    e = cudaMalloc(&d.d_bricks, sizeof(float) * brick_floats(d.dev.bshift) * d.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&d.d_brick_range, sizeof(float2) * d.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&d.d_brick_empty, d.n_bricks);
     if (e == cudaSuccess) e = cudaMemset(d.d_brick_empty, 0, d.n_bricks);
@@ -736,7 +737,7 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
       if (e != cudaSuccess) return cuda_error(e, "field copy");
       dsrc = s->stage[b];
     }
-    e = launch_brick_device(dsrc, dtype, stride, d.dev.dims, d.d_bricks, d.dev.nbrick,
+    e = launch_brick_device(dsrc, dtype, stride, d.dev.dims, d.dev.bshift, d.d_bricks, d.dev.nbrick,
                             d.d_brick_range, d_timed_out, st);
     if (e == cudaSuccess && location == GVR_MEM_HOST) e = cudaEventRecord(s->consumed[b], st);
     if (e != cudaSuccess) return cuda_error(e, "field bricking");
@@ -909,6 +910,7 @@ static int ensure_buffers(gvr_scene *s, int64_t pixels, int lut_size)
   }
   if (!s->d_counters) {
     e = cudaMalloc(&s->d_counters, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMemset(s->d_counters, 0, sizeof(unsigned long long) * 4);
     if (e != cudaSuccess) return cuda_error(e, "cudaMalloc counters");
   }
   if (pixels > s->tmp_pixels) {
@@ -1029,6 +1031,95 @@ static int tile_order(gvr_scene *s, int W, int H, const int **out)
   return GVR_OK;
 }
 
+// Front-to-back order of the domains for rays from `eye`, for the staged
+// march: domain i goes before domain j when a plane between their boxes
+// (i's upper face below j's lower face on some axis, or the reverse) has
+// the eye on i's side; every ray from the eye that crosses both boxes then
+// crosses i first. Pairs the eye sees along no such plane (it lies between
+// them, on a face plane, or the planes disagree) no ray crosses in a fixed
+// order, so they are left free. A topological sort, lowest index first
+// among the ready domains, gives the order; false when the scene is not
+// eligible (not all uniform vertex fields) or the relation has a cycle.
+static bool staged_order(const gvr_scene *s, const float eye[3], StageOrder &out)
+{
+  const int n = (int)s->domains.size();
+  if (s->has_hex || n < 1 || n > kMaxDomains) return false;
+  for (const Domain &d : s->domains)
+    if (d.dev.kind != GVR_DOMAIN_UNIFORM || d.dev.assoc != GVR_ASSOC_VERTEX ||
+        d.dev.bshift != kBrickShiftDefault)
+      return false;
+  std::vector<uint64_t> before(n, 0);   // before[j]: bits of domains that must precede j
+  for (int i = 0; i < n; ++i) {
+    for (int j = i + 1; j < n; ++j) {
+      const double *bi = s->domains[i].bounds, *bj = s->domains[j].bounds;
+      int verdict = 0;      // +1: i first, -1: j first
+      bool conflict = false;
+      for (int a = 0; a < 3; ++a) {
+        int v = 0;
+        if (bi[2 * a + 1] <= bj[2 * a]) {          // i below j on axis a
+          if (eye[a] < bi[2 * a + 1]) v = 1;
+          else if (eye[a] > bj[2 * a]) v = -1;
+        } else if (bj[2 * a + 1] <= bi[2 * a]) {   // j below i
+          if (eye[a] < bj[2 * a + 1]) v = -1;
+          else if (eye[a] > bi[2 * a]) v = 1;
+        }
+        if (v != 0) {
+          if (verdict != 0 && verdict != v) conflict = true;
+          verdict = v;
+        }
+      }
+      if (conflict || verdict == 0) continue;
+      if (verdict > 0) before[j] |= 1ull << i;
+      else before[i] |= 1ull << j;
+    }
+  }
+  uint64_t done = 0;
+  out.n = n;
+  for (int k = 0; k < n; ++k) {
+    int pick = -1;
+    for (int j = 0; j < n && pick < 0; ++j)
+      if (!(done >> j & 1) && (before[j] & ~done) == 0) pick = j;
+    if (pick < 0) return false;   // a cycle
+    out.d[k] = (unsigned char)pick;
+    done |= 1ull << pick;
+  }
+  return true;
+}
+
+int gvr_scene_set_brick_cells(gvr_scene *s, int cells)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (cells != 4 && cells != 8 && cells != 16)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "brick cells must be 4, 8 or 16");
+  for (const Domain &d : s->domains)
+    if (d.dev.kind != GVR_DOMAIN_HEX && d.dev.assoc == GVR_ASSOC_VERTEX)
+      return set_error(GVR_ERR_INVALID_ARGUMENT,
+                       "set the brick size before adding vertex-field domains");
+  s->brick_shift = cells == 4 ? 2 : (cells == 16 ? 4 : 3);
+  return GVR_OK;
+}
+
+int gvr_scene_set_staging(gvr_scene *s, int mode)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (mode != 0 && mode != 1) return set_error(GVR_ERR_INVALID_ARGUMENT, "staging mode must be 0 or 1");
+  s->tuning.staged = mode;
+  return GVR_OK;
+}
+
+int gvr_scene_staging_failures(const gvr_scene *s, uint64_t *n)
+{
+  if (!s || !n) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = 0;
+  if (!s->d_counters) return GVR_OK;
+  cudaError_t e = cudaSetDevice(s->device);
+  unsigned long long c = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&c, s->d_counters + 1, sizeof(c), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "read staging counter");
+  *n = c;
+  return GVR_OK;
+}
+
 int gvr_render_volume(gvr_scene *s, const gvr_camera *camera, const gvr_render_params *p,
                       float *rgba, float *depth, int out_location, void *stream,
                       uint64_t *samples_out)
@@ -1085,8 +1176,15 @@ static int render_one(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
   }
   const int *d_order = nullptr;
   if ((rc = tile_order(s, p->width, p->height, &d_order)) != GVR_OK) return rc;
-  e = launch_march(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
-                   samples_out ? s->d_counters : nullptr, s->tuning, s->has_hex, d_order, st);
+  StageOrder order;
+  if (s->tuning.staged && staged_order(s, camera->position, order)) {
+    e = launch_staged(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
+                      samples_out ? s->d_counters : nullptr, s->tuning, d_order, order,
+                      s->d_counters + 1, st);
+  } else {
+    e = launch_march(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,
+                     samples_out ? s->d_counters : nullptr, s->tuning, s->has_hex, d_order, st);
+  }
   if (e != cudaSuccess) return cuda_error(e, "march kernel launch");
   if (out_location == GVR_MEM_HOST) {
     e = cudaMemcpyAsync(rgba, d_rgba, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, st);

@@ -22,29 +22,31 @@ __device__ __forceinline__ float load_value(const void *src, int dtype, int64_t 
                                     : ((const float *)src)[i];
 }
 
-// One CTA per brick: gather the brick's 9^3 nodes (clamped at the domain's
-// last node), write them to the brick, and reduce their min/max.
+// One CTA per brick: gather the brick's (2^bshift + 1)^3 nodes (clamped at
+// the domain's last node), write them to the brick, and reduce their
+// min/max.
 __global__ void __launch_bounds__(256)
 brick_kernel(const void *__restrict__ src, int dtype, int64_t stride, int nx,
-             int ny, int nz, int nbx, int nby, float *__restrict__ bricks,
+             int ny, int nz, int nbx, int nby, int bshift, float *__restrict__ bricks,
              float2 *__restrict__ brick_range)
 {
   const int64_t b = blockIdx.x;
   const int bx = (int)(b % nbx);
   const int by = (int)((b / nbx) % nby);
   const int bz = (int)(b / ((int64_t)nbx * nby));
+  const int bc = brick_cells(bshift), bn = brick_nodes(bshift), bf = brick_floats(bshift);
   float vmin = FLT_MAX, vmax = -FLT_MAX;
   int bad = 0;
-  float *dst = bricks + b * kBrickFloats;
-  for (int l = threadIdx.x; l < kBrickFloats; l += blockDim.x) {
+  float *dst = bricks + b * bf;
+  for (int l = threadIdx.x; l < bf; l += blockDim.x) {
     float v = 0.f;
-    if (l < kBrickNodes * kBrickNodes * kBrickNodes) {
-      const int lx = l % kBrickNodes;
-      const int ly = (l / kBrickNodes) % kBrickNodes;
-      const int lz = l / (kBrickNodes * kBrickNodes);
-      const int x = min(bx * kBrickCells + lx, nx - 1);
-      const int y = min(by * kBrickCells + ly, ny - 1);
-      const int z = min(bz * kBrickCells + lz, nz - 1);
+    if (l < bn * bn * bn) {
+      const int lx = l % bn;
+      const int ly = (l / bn) % bn;
+      const int lz = l / (bn * bn);
+      const int x = min(bx * bc + lx, nx - 1);
+      const int y = min(by * bc + ly, ny - 1);
+      const int z = min(bz * bc + lz, nz - 1);
       const int64_t idx = ((int64_t)z * ny + y) * nx + x;
       v = load_value(src, dtype, idx * stride);
       bad |= !isfinite(v);
@@ -242,14 +244,14 @@ long long stage_first_polls()
   return n < kStageSpin ? n : kStageSpin;
 }
 
-// Brick a field in device memory: the staged kernel for contiguous float32,
-// the per-brick gather otherwise.
+// Brick a field in device memory: the staged kernel for contiguous float32
+// fields in 8^3-cell bricks, the per-brick gather otherwise.
 cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int dims[3],
-                          float *d_bricks, const int nbrick[3], float2 *d_brick_range,
+                          int bshift, float *d_bricks, const int nbrick[3], float2 *d_brick_range,
                           int *d_timed_out, cudaStream_t stream)
 {
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
-  if (dtype == GVR_DTYPE_FLOAT32 && stride == 1) {
+  if (dtype == GVR_DTYPE_FLOAT32 && stride == 1 && bshift == kBrickShiftDefault) {
     const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
     dim3 grid((unsigned)((nbrick[0] + kRunBricks - 1) / kRunBricks), (unsigned)nbrick[1],
               (unsigned)nbrick[2]);
@@ -258,7 +260,8 @@ cudaError_t launch_bricks(const void *dsrc, int dtype, int64_t stride, const int
                                                   d_timed_out, stage_first_polls());
   } else {
     brick_kernel<<<(unsigned)nb, 256, 0, stream>>>(dsrc, dtype, stride, dims[0], dims[1], dims[2],
-                                                   nbrick[0], nbrick[1], d_bricks, d_brick_range);
+                                                   nbrick[0], nbrick[1], bshift, d_bricks,
+                                                   d_brick_range);
   }
   count_launch();
   return cudaGetLastError();
@@ -351,7 +354,7 @@ cudaError_t stage_source(const void *src, int dtype, int64_t stride,
 }  // namespace
 
 cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
-                               int src_on_device, const int dims[3],
+                               int src_on_device, const int dims[3], int bshift,
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
                                Staging &stg, int *d_timed_out, bool *timed_out,
@@ -364,7 +367,8 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
   const int64_t nb = (int64_t)nbrick[0] * nbrick[1] * nbrick[2];
   e = cudaMemsetAsync(d_timed_out, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  e = launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, d_timed_out, stream);
+  e = launch_bricks(dsrc, dtype, stride, dims, bshift, d_bricks, nbrick, d_brick_range, d_timed_out,
+                    stream);
   if (e != cudaSuccess) return e;
   std::vector<float2> h((size_t)nb);
   int flag = 0;
@@ -437,11 +441,11 @@ __global__ void __launch_bounds__(1024) range_of_bricks_kernel(const RangeJobs j
 }  // namespace
 
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
-                                float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                                int *d_timed_out, cudaStream_t stream)
+                                int bshift, float *d_bricks, const int nbrick[3],
+                                float2 *d_brick_range, int *d_timed_out, cudaStream_t stream)
 {
-  return launch_bricks(dsrc, dtype, stride, dims, d_bricks, nbrick, d_brick_range, d_timed_out,
-                       stream);
+  return launch_bricks(dsrc, dtype, stride, dims, bshift, d_bricks, nbrick, d_brick_range,
+                       d_timed_out, stream);
 }
 
 cudaError_t launch_ranges_of_bricks(int n, const float2 *const *brick_ranges,

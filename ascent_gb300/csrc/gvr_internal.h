@@ -22,6 +22,19 @@ constexpr int kBrickNodes = kBrickCells + 1;
 constexpr int kBrickFloats = 736;
 static_assert(kBrickNodes * kBrickNodes * kBrickNodes <= kBrickFloats, "brick");
 
+// A scene may brick its fields with 4^3, 8^3 (the default above) or 16^3
+// cells per brick (gvr_scene_set_brick_cells; the autotuner picks one). A
+// brick of 2^shift cells per axis stores (2^shift + 1)^3 nodes, padded to a
+// multiple of 32 floats (128 bytes): 128, 736 or 4928 floats.
+constexpr int kBrickShiftMin = 2, kBrickShiftMax = 4, kBrickShiftDefault = 3;
+__host__ __device__ constexpr int brick_cells(int shift) { return 1 << shift; }
+__host__ __device__ constexpr int brick_nodes(int shift) { return (1 << shift) + 1; }
+__host__ __device__ constexpr int brick_floats(int shift)
+{
+  return (brick_nodes(shift) * brick_nodes(shift) * brick_nodes(shift) + 31) / 32 * 32;
+}
+static_assert(brick_floats(kBrickShiftDefault) == kBrickFloats, "default brick");
+
 constexpr int kMaxDomains = 64;     // domains a single render can composite
 constexpr int kMaxLut = 4096;
 constexpr int kMarchTile = 16;      // march kernel: one CTA per 16x16-pixel tile
@@ -50,7 +63,7 @@ struct DomainDev {
   const int *hex_ids;         // cell id of each sorted leaf
   const int *hex_nbr;         // 6 face neighbours per cell (r=0,r=1,s=0,s=1,t=0,t=1), -1 none
   int n_cells;
-  int pad_;
+  int bshift;                 // vertex fields: 2^bshift cells per brick axis
 };
 
 // Launch shape of the march kernel (picked by the autotuner): pixel packet
@@ -61,6 +74,13 @@ struct Tuning {
   int unroll = 2;
   int min_blocks = 4;
   int tiles_per_item = 1;   // batch path: 16x16 tiles per work-queue item
+  int staged = 0;           // plain path: stage bricks in shared memory (uniform vertex scenes)
+};
+
+// Front-to-back order of a scene's domains for one view (staged march).
+struct StageOrder {
+  int n;
+  unsigned char d[kMaxDomains];
 };
 
 // Everything the march kernel needs for one view.
@@ -142,6 +162,7 @@ struct Domain {
 
 struct gvr_scene {
   int device = 0;
+  int brick_shift = gvr::kBrickShiftDefault;  // bricks of vertex fields added from now on
   std::vector<gvr::Domain> domains;
   gvr::DomainDev *d_domains = nullptr;   // device copy of the domain table
   int d_domains_cap = 0;
@@ -149,7 +170,7 @@ struct gvr_scene {
   int *d_any_empty = nullptr;            // per-domain empty-brick flags
   bool has_hex = false;
   gvr::Tuning tuning;
-  unsigned long long *d_counters = nullptr;  // [0] samples
+  unsigned long long *d_counters = nullptr;  // [0] samples, [1] staged waits given up
   float4 *d_rgba_tmp = nullptr;          // device image for host outputs
   float *d_depth_tmp = nullptr;
   int64_t tmp_pixels = 0;
@@ -218,7 +239,7 @@ uint64_t launch_count();
 // *d_timed_out is a device int the staged kernel sets when a bulk copy did
 // not complete within its bounded wait; *timed_out receives it.
 cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
-                               int src_on_device, const int dims[3],
+                               int src_on_device, const int dims[3], int bshift,
                                float *d_bricks, const int nbrick[3],
                                float2 *d_brick_range, double range_out[2],
                                Staging &stg, int *d_timed_out, bool *timed_out,
@@ -227,8 +248,8 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
 // ranges (no host synchronisation); a staged copy that gives up waiting
 // sets *d_timed_out.
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
-                                float *d_bricks, const int nbrick[3], float2 *d_brick_range,
-                                int *d_timed_out, cudaStream_t stream);
+                                int bshift, float *d_bricks, const int nbrick[3],
+                                float2 *d_brick_range, int *d_timed_out, cudaStream_t stream);
 // Reduce n domains' per-brick ranges to one range each (*out[j]; NaN when a
 // brick holds a non-finite value): one launch, one block per domain.
 cudaError_t launch_ranges_of_bricks(int n, const float2 *const *brick_ranges,
@@ -264,6 +285,14 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          float4 *d_rgba, float *d_depth,
                          unsigned long long *d_samples, const Tuning &tuning,
                          bool has_hex, const int *d_order, cudaStream_t stream);
+// staged march (gvr_march.cu): uniform vertex-field domains only, taken in
+// `order`; *d_stage_fail counts CTAs whose bounded wait for their bulk
+// copies gave up (they finish from global memory)
+cudaError_t launch_staged(const DomainDev *d_domains, const ViewDev &view, const MarchParams &mp,
+                          const float4 *d_lut, float4 *d_rgba, float *d_depth,
+                          unsigned long long *d_samples, const Tuning &tuning, const int *d_order,
+                          const StageOrder &order, unsigned long long *d_stage_fail,
+                          cudaStream_t stream);
 cudaError_t batch_grid(const MarchParams &mp, int n_views, const Tuning &tuning, bool has_hex,
                        int *grid);
 cudaError_t launch_batch(const DomainDev *d_domains, const ViewDev *d_views, const int4 *d_rects,

@@ -88,14 +88,22 @@ __device__ __forceinline__ int rect_cell(const float *__restrict__ x, int n, flo
   return i;
 }
 
-// March one structured domain over [t0, t1): accumulates the domain's
-// partial in acc and returns the number of samples the stepping rule takes.
-__device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, float t0, float t1,
-                            const MarchParams &mp, const float4 *lut, float thr,
-                            float4 &acc)
+struct Partial {
+  float4 acc;   // premultiplied colour and opacity of the domain's partial
+  int count;    // samples the stepping rule took
+};
+
+// March one structured domain over [t0, t1) from zero opacity: the domain's
+// partial and its sample count. Not inlined (the general path: rectilinear
+// coordinates, element fields), so that its registers do not weigh on the
+// kernels' uniform-grid loop; the ray comes by value and the result goes
+// back by value, so nothing is kept in local memory for the call.
+__device__ __noinline__ Partial march_domain(const DomainDev &dm, const Ray r, float t0, float t1,
+                                             const MarchParams &mp, const float4 *lut, float thr)
 {
   const float dt = mp.sample_dist;
   int count = 0;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   const int nx = dm.dims[0], ny = dm.dims[1], nz = dm.dims[2];
   const float gmax[3] = {(float)(nx - 1), (float)(ny - 1), (float)(nz - 1)};
   // grid coordinates g = A + t B (uniform)
@@ -120,6 +128,7 @@ __device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, floa
     }
   }
   const int nbx = dm.nbrick[0], nby = dm.nbrick[1];
+  const int bsh = dm.bshift, bc = brick_cells(bsh), bn = brick_nodes(bsh), bf = brick_floats(bsh);
   const float inv_dt = 1.f / dt;
   for (int k = 0;; ++k) {
     const float t = fmaf((float)k, dt, t0);
@@ -149,7 +158,7 @@ __device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, floa
     if (dm.assoc == GVR_ASSOC_ELEMENT) {
       v = __ldg(dm.cells + ((int64_t)c[2] * (ny - 1) + c[1]) * (nx - 1) + c[0]);
     } else {
-      const int bx = c[0] >> 3, by = c[1] >> 3, bz = c[2] >> 3;
+      const int bx = c[0] >> bsh, by = c[1] >> bsh, bz = c[2] >> bsh;
       const int64_t brick = ((int64_t)bz * nby + by) * nbx + bx;
       if (mp.skip_empty && dm.brick_empty[brick]) {
         // Empty brick: every sample inside it has zero opacity. Jump to the
@@ -159,8 +168,8 @@ __device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, floa
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           if (dm.kind == GVR_DOMAIN_UNIFORM && B[a] != 0.f) {
-            const float edge = B[a] > 0.f ? (float)min((b3[a] + 1) * kBrickCells, dm.dims[a] - 1)
-                                          : (float)(b3[a] * kBrickCells);
+            const float edge = B[a] > 0.f ? (float)min((b3[a] + 1) * bc, dm.dims[a] - 1)
+                                          : (float)(b3[a] * bc);
             texit = fminf(texit, (edge - A[a]) / B[a]);
           }
         }
@@ -175,14 +184,14 @@ __device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, floa
         }
         continue;
       }
-      const float *p = dm.bricks + brick * kBrickFloats +
-                       ((c[2] & 7) * kBrickNodes + (c[1] & 7)) * kBrickNodes + (c[0] & 7);
+      const int m = bc - 1;
+      const float *p = dm.bricks + brick * bf + ((c[2] & m) * bn + (c[1] & m)) * bn + (c[0] & m);
       const float v000 = __ldg(p), v100 = __ldg(p + 1);
-      const float v010 = __ldg(p + kBrickNodes), v110 = __ldg(p + kBrickNodes + 1);
-      const float v001 = __ldg(p + kBrickNodes * kBrickNodes);
-      const float v101 = __ldg(p + kBrickNodes * kBrickNodes + 1);
-      const float v011 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
-      const float v111 = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+      const float v010 = __ldg(p + bn), v110 = __ldg(p + bn + 1);
+      const float v001 = __ldg(p + bn * bn);
+      const float v101 = __ldg(p + bn * bn + 1);
+      const float v011 = __ldg(p + bn * bn + bn);
+      const float v111 = __ldg(p + bn * bn + bn + 1);
       const float c00 = lerpf(v000, v100, w[0]);
       const float c10 = lerpf(v010, v110, w[0]);
       const float c01 = lerpf(v001, v101, w[0]);
@@ -200,7 +209,7 @@ __device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, floa
     acc.w += wa;
     if (acc.w >= thr) break;
   }
-  return count;
+  return Partial{acc, count};
 }
 
 
@@ -210,7 +219,7 @@ __device__ __noinline__ int march_domain(const DomainDev &dm, const Ray &r, floa
 // before it reuses that cell's corners from registers (the same values, so
 // the result does not change). Blending stays sequential and stops exactly
 // where the one-sample loop stops.
-template <int UNROLL>
+template <int UNROLL, int SH>
 __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, float t0,
                                              float t1, const MarchParams &mp,
                                              const float4 *lut, float thr, float4 &acc)
@@ -223,7 +232,8 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
     B[a] = r.d[a] * dm.inv_spacing[a];
   }
   const int cmax[3] = {dm.dims[0] - 2, dm.dims[1] - 2, dm.dims[2] - 2};
-  const int sy = dm.nbrick[0] * kBrickFloats;
+  constexpr int BC = brick_cells(SH), BN = brick_nodes(SH), BF = brick_floats(SH);
+  const int sy = dm.nbrick[0] * BF;
   const int sz = dm.nbrick[1] * sy;
   const float *__restrict__ bricks = dm.bricks;
   const float nm1 = (float)(mp.lut_size - 1);
@@ -247,20 +257,20 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
         const float g = fmaf(t, B[a], A[a]);
         const int c = max(0, min((int)g, cmax[a]));
         w[a] = g - (float)c;
-        const int hi = c >> 3, lo = c & 7;
-        off += a == 0 ? hi * kBrickFloats + lo
-                      : (a == 1 ? hi * sy + lo * kBrickNodes : hi * sz + lo * kBrickNodes * kBrickNodes);
+        const int hi = c >> SH, lo = c & (BC - 1);
+        off += a == 0 ? hi * BF + lo
+                      : (a == 1 ? hi * sy + lo * BN : hi * sz + lo * BN * BN);
       }
       if (off != last_off) {
         const float *p = bricks + off;
         lc[0] = __ldg(p);
         lc[1] = __ldg(p + 1);
-        lc[2] = __ldg(p + kBrickNodes);
-        lc[3] = __ldg(p + kBrickNodes + 1);
-        lc[4] = __ldg(p + kBrickNodes * kBrickNodes);
-        lc[5] = __ldg(p + kBrickNodes * kBrickNodes + 1);
-        lc[6] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
-        lc[7] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+        lc[2] = __ldg(p + BN);
+        lc[3] = __ldg(p + BN + 1);
+        lc[4] = __ldg(p + BN * BN);
+        lc[5] = __ldg(p + BN * BN + 1);
+        lc[6] = __ldg(p + BN * BN + BN);
+        lc[7] = __ldg(p + BN * BN + BN + 1);
         last_off = off;
       }
       const float c00 = lerpf(lc[0], lc[1], w[0]);
@@ -297,7 +307,7 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
 // and a non-empty brick's samples up to its exit run through the same
 // unrolled, corner-reusing loop as march_uniform. Compared with a test per
 // sample, the emptiness test and the exit distance are paid once per brick.
-template <int UNROLL>
+template <int UNROLL, int SH>
 __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, float t0,
                                          float t1, const MarchParams &mp,
                                          const float4 *lut, float thr, float4 &acc)
@@ -310,7 +320,8 @@ __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, f
     B[a] = r.d[a] * dm.inv_spacing[a];
   }
   const int cmax[3] = {dm.dims[0] - 2, dm.dims[1] - 2, dm.dims[2] - 2};
-  const int sy = dm.nbrick[0] * kBrickFloats;
+  constexpr int BC = brick_cells(SH), BN = brick_nodes(SH), BF = brick_floats(SH);
+  const int sy = dm.nbrick[0] * BF;
   const int sz = dm.nbrick[1] * sy;
   const float *__restrict__ bricks = dm.bricks;
   const float nm1 = (float)(mp.lut_size - 1);
@@ -325,10 +336,10 @@ __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, f
     float texit = t1;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      b[a] = max(0, min((int)fmaf(t, B[a], A[a]), cmax[a])) >> 3;
+      b[a] = max(0, min((int)fmaf(t, B[a], A[a]), cmax[a])) >> SH;
       if (B[a] != 0.f) {
-        const float edge = B[a] > 0.f ? (float)min((b[a] + 1) * kBrickCells, cmax[a] + 1)
-                                      : (float)(b[a] * kBrickCells);
+        const float edge = B[a] > 0.f ? (float)min((b[a] + 1) * BC, cmax[a] + 1)
+                                      : (float)(b[a] * BC);
         texit = fminf(texit, (edge - A[a]) / B[a]);
       }
     }
@@ -356,20 +367,20 @@ __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, f
           const float g = fmaf(ts, B[a], A[a]);
           const int c = max(0, min((int)g, cmax[a]));
           w[a] = g - (float)c;
-          const int hi = c >> 3, lo = c & 7;
-          off += a == 0 ? hi * kBrickFloats + lo
-                        : (a == 1 ? hi * sy + lo * kBrickNodes : hi * sz + lo * kBrickNodes * kBrickNodes);
+          const int hi = c >> SH, lo = c & (BC - 1);
+          off += a == 0 ? hi * BF + lo
+                        : (a == 1 ? hi * sy + lo * BN : hi * sz + lo * BN * BN);
         }
         if (off != last_off) {
           const float *p = bricks + off;
           lc[0] = __ldg(p);
           lc[1] = __ldg(p + 1);
-          lc[2] = __ldg(p + kBrickNodes);
-          lc[3] = __ldg(p + kBrickNodes + 1);
-          lc[4] = __ldg(p + kBrickNodes * kBrickNodes);
-          lc[5] = __ldg(p + kBrickNodes * kBrickNodes + 1);
-          lc[6] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes);
-          lc[7] = __ldg(p + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+          lc[2] = __ldg(p + BN);
+          lc[3] = __ldg(p + BN + 1);
+          lc[4] = __ldg(p + BN * BN);
+          lc[5] = __ldg(p + BN * BN + 1);
+          lc[6] = __ldg(p + BN * BN + BN);
+          lc[7] = __ldg(p + BN * BN + BN + 1);
           last_off = off;
         }
         const float c00 = lerpf(lc[0], lc[1], w[0]);
@@ -496,12 +507,10 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
 // g_state: the CTA's shared-memory slots for the state that must survive
 // the march of a domain (kStateSlots words per thread, slot k of thread i
 // at g_state[k * kThreads + i]).
-template <int UNROLL, bool HEX>
-__device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, const ViewDev &view,
-                                          const MarchParams &mp, const float4 *lut, int px, int py,
-                                          float4 &out, float &dep, float *g_state)
+// The ray of pixel (px, py): the pinhole model partials_to_canvas inverts
+// (VolumeRenderer.cpp:335-344).
+__device__ __forceinline__ Ray pixel_ray(const ViewDev &view, const MarchParams &mp, int px, int py)
 {
-  int count = 0;
   Ray r;
   const float fx = view.dx_scale * ((float)px - 0.5f * (float)mp.width - view.xoff);
   const float fy = view.dy_scale * ((float)py - 0.5f * (float)mp.height - view.yoff);
@@ -517,10 +526,16 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
     r.o[a] = view.origin[a];
     r.d[a] = d[a] * inv;
   }
+  return r;
+}
 
-  // Opaque canvas: the ray ends at the world point of the canvas depth
-  // (MapCanvasToRays: pixel (i, j) at depth d unprojected from NDC
-  // (2i/W - 1, 2j/H - 1, 2d - 1); FP64, as in the oracle).
+// Opaque canvas: the ray ends at the world point of the canvas depth
+// (MapCanvasToRays: pixel (i, j) at depth d unprojected from NDC
+// (2i/W - 1, 2j/H - 1, 2d - 1); FP64, as in the oracle). FLT_MAX without a
+// canvas.
+__device__ __forceinline__ float canvas_ray_end(const ViewDev &view, const MarchParams &mp, int px,
+                                                int py)
+{
   float t_max = FLT_MAX;
   if (mp.canvas_depth) {
     const int64_t pix = (int64_t)py * mp.width + px;
@@ -537,6 +552,71 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
       t_max = (float)sqrt(ex * ex + ey * ey + ez * ez);
     }
   }
+  return t_max;
+}
+
+// The pixel's final value from its composited partial (have = whether any
+// partial survived the cull): partials_to_canvas over the cleared or opaque
+// canvas with the image depth, then the uint8 round trip and background.
+__device__ __forceinline__ void finish_pixel(const ViewDev &view, const MarchParams &mp, int px, int py,
+                                             bool have, const float crgb[3], float ca, float cdepth,
+                                             float4 &out, float &dep)
+{
+  float4 cin = make_float4(0.f, 0.f, 0.f, 0.f);
+  float din = mp.clear_depth;
+  if (mp.canvas_depth) {
+    const int64_t pix = (int64_t)py * mp.width + px;
+    cin = mp.canvas_rgba[pix];
+    din = mp.canvas_depth[pix];
+  }
+  out = cin;
+  dep = din;
+  if (have) {
+    const float om = 1.f - ca;
+    out = make_float4(crgb[0] + cin.x * om, crgb[1] + cin.y * om, crgb[2] + cin.z * om,
+                      cin.w * om + ca);
+    // partials_to_canvas ray rebuild: delta_y runs along ru there
+    const float ex = view.dx_scale * (float)(2 * px - mp.width) * 0.5f;
+    const float ey = view.dy_scale * (float)(2 * py - mp.height) * 0.5f;
+    float q[3], qn = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      q[a] = view.look[a] + view.ru[a] * ex + view.ru[a] * ey;
+      qn = fmaf(q[a], q[a], qn);
+    }
+    const float qi = rsqrtf(qn);
+    float pos[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] = fmaf(cdepth, q[a] * qi, view.origin[a]);
+    const float *M = view.projview;
+    const float z = M[8] * pos[0] + M[9] * pos[1] + M[10] * pos[2] + M[11];
+    const float wv = M[12] * pos[0] + M[13] * pos[1] + M[14] * pos[2] + M[15];
+    dep = 0.5f * (z / wv) + 0.49f;
+  }
+  if (mp.quantize_uint8) {
+    out.x = (float)(unsigned char)fminf(out.x * 255.f, 255.f) * (1.f / 255.f);
+    out.y = (float)(unsigned char)fminf(out.y * 255.f, 255.f) * (1.f / 255.f);
+    out.z = (float)(unsigned char)fminf(out.z * 255.f, 255.f) * (1.f / 255.f);
+    out.w = (float)(unsigned char)fminf(out.w * 255.f, 255.f) * (1.f / 255.f);
+    dep = fabsf(dep);
+  }
+  if (mp.render_bg) {
+    const float om = 1.f - out.w;
+    out.x = fmaf(mp.bg[0], om, out.x);
+    out.y = fmaf(mp.bg[1], om, out.y);
+    out.z = fmaf(mp.bg[2], om, out.z);
+    out.w = fmaf(mp.bg[3], om, out.w);
+  }
+}
+
+template <int UNROLL, bool HEX>
+__device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, const ViewDev &view,
+                                          const MarchParams &mp, const float4 *lut, int px, int py,
+                                          float4 &out, float &dep, float *g_state)
+{
+  int count = 0;
+  const Ray r = pixel_ray(view, mp, px, py);
+  const float t_max = canvas_ray_end(view, mp, px, py);
 
   // Compositing state that lives across the march of a domain is parked in
   // shared memory (one word per thread per slot, st[k * kThreads]), so the
@@ -592,11 +672,18 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
       count += march_hex(dm, r, bt0, bt1, mp, lut, thr, acc);
     else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
              !(mp.skip_empty && *dm.any_empty))
-      count += march_uniform<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
+      count += dm.bshift == 3 ? march_uniform<UNROLL, 3>(dm, r, bt0, bt1, mp, lut, thr, acc)
+             : dm.bshift == 2 ? march_uniform<UNROLL, 2>(dm, r, bt0, bt1, mp, lut, thr, acc)
+                              : march_uniform<UNROLL, 4>(dm, r, bt0, bt1, mp, lut, thr, acc);
     else if (dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX)
-      count += march_bricks<UNROLL>(dm, r, bt0, bt1, mp, lut, thr, acc);
-    else
-      count += march_domain(dm, r, bt0, bt1, mp, lut, thr, acc);
+      count += dm.bshift == 3 ? march_bricks<UNROLL, 3>(dm, r, bt0, bt1, mp, lut, thr, acc)
+             : dm.bshift == 2 ? march_bricks<UNROLL, 2>(dm, r, bt0, bt1, mp, lut, thr, acc)
+                              : march_bricks<UNROLL, 4>(dm, r, bt0, bt1, mp, lut, thr, acc);
+    else {
+      const Partial part = march_domain(dm, r, bt0, bt1, mp, lut, thr);
+      acc = part.acc;
+      count += part.count;
+    }
     if (acc.w < mp.alpha_cull) continue;
     if (!have) {
       st[0 * kThreads] = acc.x; st[1 * kThreads] = acc.y; st[2 * kThreads] = acc.z;
@@ -616,60 +703,15 @@ __device__ __forceinline__ int render_ray(const DomainDev *doms, uint64_t mask, 
   px = __float_as_int(st[8 * kThreads]);
   py = __float_as_int(st[9 * kThreads]);
 
-  // partials_to_canvas: the composited partial in front of the canvas
-  float4 cin = make_float4(0.f, 0.f, 0.f, 0.f);
-  float din = mp.clear_depth;
-  if (mp.canvas_depth) {
-    const int64_t pix = (int64_t)py * mp.width + px;
-    cin = mp.canvas_rgba[pix];
-    din = mp.canvas_depth[pix];
-  }
-  out = cin;
-  dep = din;
-  if (have) {
-    const float om = 1.f - ca;
-    out = make_float4(crgb[0] + cin.x * om, crgb[1] + cin.y * om, crgb[2] + cin.z * om,
-                      cin.w * om + ca);
-    // partials_to_canvas ray rebuild: delta_y runs along ru there
-    const float ex = view.dx_scale * (float)(2 * px - mp.width) * 0.5f;
-    const float ey = view.dy_scale * (float)(2 * py - mp.height) * 0.5f;
-    float q[3], qn = 0.f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      q[a] = view.look[a] + view.ru[a] * ex + view.ru[a] * ey;
-      qn = fmaf(q[a], q[a], qn);
-    }
-    const float qi = rsqrtf(qn);
-    float pos[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) pos[a] = fmaf(cdepth, q[a] * qi, view.origin[a]);
-    const float *M = view.projview;
-    const float z = M[8] * pos[0] + M[9] * pos[1] + M[10] * pos[2] + M[11];
-    const float wv = M[12] * pos[0] + M[13] * pos[1] + M[14] * pos[2] + M[15];
-    dep = 0.5f * (z / wv) + 0.49f;
-  }
-  if (mp.quantize_uint8) {
-    out.x = (float)(unsigned char)fminf(out.x * 255.f, 255.f) * (1.f / 255.f);
-    out.y = (float)(unsigned char)fminf(out.y * 255.f, 255.f) * (1.f / 255.f);
-    out.z = (float)(unsigned char)fminf(out.z * 255.f, 255.f) * (1.f / 255.f);
-    out.w = (float)(unsigned char)fminf(out.w * 255.f, 255.f) * (1.f / 255.f);
-    dep = fabsf(dep);
-  }
-  if (mp.render_bg) {
-    const float om = 1.f - out.w;
-    out.x = fmaf(mp.bg[0], om, out.x);
-    out.y = fmaf(mp.bg[1], om, out.y);
-    out.z = fmaf(mp.bg[2], om, out.z);
-    out.w = fmaf(mp.bg[3], om, out.w);
-  }
+  finish_pixel(view, mp, px, py, have, crgb, ca, cdepth, out, dep);
   return count;
 }
 
 // PW x (32 / PW) pixel packet per warp, 16 x 16 pixels per CTA.
 template <int PW, int UNROLL, int MINB, bool HEX = false>
 __global__ void __launch_bounds__(kThreads, MINB)
-march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
-             const MarchParams mp, const float4 *__restrict__ g_lut,
+march_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ ViewDev view,
+             const __grid_constant__ MarchParams mp, const float4 *__restrict__ g_lut,
              float4 *__restrict__ rgba, float *__restrict__ depth,
              unsigned long long *__restrict__ samples, const int *__restrict__ order)
 {
@@ -714,6 +756,430 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
 }
 
 
+// ---------------------------------------------------------------------------
+// Shared-memory staged march (uniform grids, vertex fields).
+//
+// The CTA's 256 rays form a thin frustum (its 16 x 16 tile). The kernel walks
+// the frustum in slabs of ray distance [T, T + dT): for each slab it lists
+// the bricks of the current domain that the frustum crosses there (a plane
+// test of every brick in the slab's bounding box against the frustum's four
+// side planes and its near and far planes), copies them into shared memory
+// with one bulk copy each (cp.async.bulk, 2944 contiguous bytes, completing
+// on an mbarrier with a bounded wait), and then every ray takes its samples
+// of the slab from shared memory. dT is the deepest of {8, 4, 2, 1, 1/2, 1/4}
+// brick edges whose box of candidate bricks fits the map and whose frustum
+// bricks fit the kStageSlots slots. Bricks whose LUT opacity is zero over
+// their range are not copied: their samples are counted and skipped, as the
+// brick-walking march does. A brick the plan did not stage (frustum test
+// rounding, slots full) is read from global memory, so the plan never
+// changes a pixel.
+//
+// Domains are taken in one front-to-back order for the whole CTA (computed on
+// the host per view from the planes that separate the domains' boxes, see
+// staged_order in gvr_api.cpp). For boxes that do not overlap, every ray that
+// crosses two of them crosses them in that order, so each ray composites its
+// partials in the order the per-ray walk of render_ray would choose, with the
+// same per-sample arithmetic: the images are bit-identical to march_kernel's.
+// ---------------------------------------------------------------------------
+constexpr int kStageSlots = 24;           // staged bricks per slab (24 x 2944 B = 69 KB)
+constexpr int kStageMap = 1024;           // bricks in a slab's candidate box
+constexpr long long kStagePolls = 1ll << 20;  // bounded mbarrier wait (polls)
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool stage_wait(const uint64_t *bar, unsigned phase, long long polls)
+{
+  for (long long i = 0; i < polls; ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    if (ok) return true;
+    if (i > 32) __nanosleep(32);
+  }
+  return false;
+}
+
+// Frustum of a tile: ray origin, unit centre direction, the cosine of the
+// widest corner ray against it, and four inward side-plane normals through
+// the origin (corner rays at the tile's outer pixel edges).
+struct Frustum {
+  float o[3];
+  float c[3];
+  float cos_min;
+  float n[4][3];
+  float dn[4][3];   // unit corner directions
+};
+
+__device__ void tile_frustum(const ViewDev &view, const MarchParams &mp, int x0, int y0, Frustum &f)
+{
+  auto dir = [&](float x, float y, float d[3]) {
+    const float fx = view.dx_scale * (x - 0.5f * (float)mp.width - view.xoff);
+    const float fy = view.dy_scale * (y - 0.5f * (float)mp.height - view.yoff);
+    float n2 = 0.f;
+    for (int a = 0; a < 3; ++a) {
+      d[a] = view.look[a] + view.ru[a] * fx + view.rv[a] * fy;
+      n2 += d[a] * d[a];
+    }
+    const float inv = rsqrtf(n2);
+    for (int a = 0; a < 3; ++a) d[a] *= inv;
+  };
+  const float xa = (float)x0 - 0.5f, xb = (float)(x0 + kTile - 1) + 0.5f;
+  const float ya = (float)y0 - 0.5f, yb = (float)(y0 + kTile - 1) + 0.5f;
+  dir(xa, ya, f.dn[0]);
+  dir(xb, ya, f.dn[1]);
+  dir(xb, yb, f.dn[2]);
+  dir(xa, yb, f.dn[3]);
+  dir(0.5f * (xa + xb), 0.5f * (ya + yb), f.c);
+  for (int a = 0; a < 3; ++a) f.o[a] = view.origin[a];
+  f.cos_min = 1.f;
+  for (int i = 0; i < 4; ++i) {
+    const float *u = f.dn[i], *v = f.dn[(i + 1) & 3];
+    float nn[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+    const float side = nn[0] * f.c[0] + nn[1] * f.c[1] + nn[2] * f.c[2];
+    for (int a = 0; a < 3; ++a) f.n[i][a] = side < 0.f ? -nn[a] : nn[a];
+    f.cos_min = fminf(f.cos_min, u[0] * f.c[0] + u[1] * f.c[1] + u[2] * f.c[2]);
+  }
+  f.cos_min -= 1e-6f;
+}
+
+// Could the frustum's points at ray distance [t0, t1] lie in the box? (No
+// false negatives beyond float rounding; a brick wrongly rejected is read
+// from global memory.)
+__device__ __forceinline__ bool frustum_box(const Frustum &f, float t0, float t1, const float lo[3],
+                                            const float hi[3])
+{
+  for (int i = 0; i < 4; ++i) {
+    float m = 0.f;
+    for (int a = 0; a < 3; ++a) m += f.n[i][a] * ((f.n[i][a] > 0.f ? hi[a] : lo[a]) - f.o[a]);
+    if (m < 0.f) return false;
+  }
+  float zmax = 0.f, zmin = 0.f;
+  for (int a = 0; a < 3; ++a) {
+    zmax += f.c[a] * ((f.c[a] > 0.f ? hi[a] : lo[a]) - f.o[a]);
+    zmin += f.c[a] * ((f.c[a] > 0.f ? lo[a] : hi[a]) - f.o[a]);
+  }
+  return zmax >= t0 * f.cos_min && zmin <= t1;
+}
+
+template <int PW>
+__global__ void __launch_bounds__(kThreads, 2)
+staged_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ ViewDev view,
+              const __grid_constant__ MarchParams mp,
+              const float4 *__restrict__ g_lut, float4 *__restrict__ rgba, float *__restrict__ depth,
+              unsigned long long *__restrict__ samples, const int *__restrict__ order,
+              const StageOrder dorder, unsigned long long *__restrict__ stage_fail)
+{
+  constexpr int PH = 32 / PW;
+  constexpr int PX = kTile / PW;
+  const int tiles_x = (mp.width + kTile - 1) / kTile;
+  const int tile = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
+  const int tile_x = tile % tiles_x, tile_y = tile / tiles_x;
+  extern __shared__ float4 smem[];
+  float4 *lut = smem;
+  DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
+  const size_t head = ((sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains) + 127) & ~(size_t)127;
+  float *slots = reinterpret_cast<float *>(reinterpret_cast<char *>(smem) + head);
+  __shared__ short s_map[kStageMap];
+  __shared__ int s_list[kStageSlots];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ Frustum s_fr;
+  __shared__ int s_box[6];      // first brick and extent of the slab's candidate box
+  __shared__ int s_count;       // frustum bricks found (may exceed the slots)
+  __shared__ int s_level;       // slab depth level of the plan
+  __shared__ float s_t1;        // slab end
+  __shared__ unsigned s_tmin;   // next sample distance of the CTA's live rays (bits)
+
+  for (int i = threadIdx.x; i < mp.lut_size; i += kThreads) lut[i] = g_lut[i];
+  {
+    const int words = mp.n_domains * (int)(sizeof(DomainDev) / 4);
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(g_domains);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(doms);
+    for (int i = threadIdx.x; i < words; i += kThreads) dst[i] = src[i];
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tile_frustum(view, mp, tile_x * kTile, tile_y * kTile, s_fr);
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int px = tile_x * kTile + (warp % PX) * PW + (lane % PW);
+  const int py = tile_y * kTile + (warp / PX) * PH + (lane / PW);
+  const bool valid = px < mp.width && py < mp.height;
+  const Ray r = pixel_ray(view, mp, valid ? px : 0, valid ? py : 0);
+  const float t_max = valid ? canvas_ray_end(view, mp, px, py) : FLT_MAX;
+  const float dt = mp.sample_dist;
+  const float nm1 = (float)(mp.lut_size - 1);
+
+  float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f, covered = -FLT_MAX;
+  bool have = false;
+  int count = 0;
+  unsigned phase = 0;
+  bool staging = true;          // CTA-uniform: off after a wait gave up
+
+  for (int oi = 0; oi < dorder.n; ++oi) {
+    const DomainDev &dm = doms[dorder.d[oi]];
+    // this ray's interval in the domain, as render_ray clamps it
+    float bt0 = 0.f, bt1 = 0.f;
+    bool act = false;
+    if (valid && ca < mp.early_term) {
+      float t0, t1;
+      if (slab(dm, r, t0, t1)) {
+        bt0 = fmaxf(t0, covered);
+        bt1 = fminf(t1, t_max);
+        covered = fmaxf(covered, bt1);
+        act = true;
+      }
+    }
+    if (!__syncthreads_or(act)) continue;
+    const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float A[3], B[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      A[a] = (r.o[a] - dm.origin[a]) * dm.inv_spacing[a];
+      B[a] = r.d[a] * dm.inv_spacing[a];
+    }
+    const int cmax[3] = {dm.dims[0] - 2, dm.dims[1] - 2, dm.dims[2] - 2};
+    const int nbx = dm.nbrick[0], nby = dm.nbrick[1];
+    const bool skip = mp.skip_empty && *dm.any_empty;
+    int k = 0;
+    bool live = act;
+    int last_off = -1;
+    float lc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (threadIdx.x == 0) s_level = 2;
+    for (;;) {
+      // the CTA's next sample distance
+      float tn = FLT_MAX;
+      if (live) {
+        tn = fmaf((float)k, dt, bt0);
+        if (!(tn < bt1)) {
+          live = false;
+          tn = FLT_MAX;
+        }
+      }
+      if (threadIdx.x == 0) s_tmin = __float_as_uint(FLT_MAX);
+      __syncthreads();
+      if (live) atomicMin(&s_tmin, __float_as_uint(fmaxf(tn, 0.f)));
+      __syncthreads();
+      const float T = __uint_as_float(s_tmin);
+      if (!(T < FLT_MAX)) break;
+
+      // plan the slab: depth level, candidate box, frustum bricks -> slots
+      const float brick_w = 8.f * fminf(fminf(1.f / dm.inv_spacing[0], 1.f / dm.inv_spacing[1]),
+                                        1.f / dm.inv_spacing[2]);
+      for (;;) {
+        if (threadIdx.x == 0) {
+          int lvl = s_level;
+          for (;; ++lvl) {
+            const float dT = brick_w * (float)(8 >> min(lvl, 3)) / (float)(1 << max(lvl - 3, 0));
+            // (a slab that would not advance past T in float covers the rest)
+            const float t1 = T + dT > T ? T + dT : FLT_MAX;
+            float gmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, gmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            for (int q = 0; q < 9; ++q) {
+              const float *dd = q < 8 ? s_fr.dn[q & 3] : s_fr.c;
+              const float tq = q < 4 ? T : t1;
+              for (int a = 0; a < 3; ++a) {
+                const float g = (fmaf(tq, dd[a], s_fr.o[a]) - dm.origin[a]) * dm.inv_spacing[a];
+                gmin[a] = fminf(gmin[a], g);
+                gmax[a] = fmaxf(gmax[a], g);
+              }
+            }
+            int nb = 1;
+            for (int a = 0; a < 3; ++a) {
+              const int c0 = max(0, min((int)floorf(fmaxf(gmin[a], -1.f)) - 1, cmax[a]));
+              const int c1 = max(0, min((int)floorf(fminf(gmax[a], (float)cmax[a] + 2.f)) + 1, cmax[a]));
+              s_box[a] = c0 >> 3;
+              s_box[3 + a] = (c1 >> 3) - (c0 >> 3) + 1;
+              nb *= s_box[3 + a];
+            }
+            s_t1 = t1;
+            if (nb <= kStageMap || lvl >= 5) {
+              if (nb > kStageMap) s_box[3] = s_box[4] = s_box[5] = 0;  // no map: global reads
+              s_level = lvl;
+              break;
+            }
+          }
+          s_count = 0;
+        }
+        __syncthreads();
+        const int nb = s_box[3] * s_box[4] * s_box[5];
+        for (int i = threadIdx.x; i < nb; i += kThreads) {
+          const int bx = s_box[0] + i % s_box[3];
+          const int by = s_box[1] + (i / s_box[3]) % s_box[4];
+          const int bz = s_box[2] + i / (s_box[3] * s_box[4]);
+          const int64_t gi = ((int64_t)bz * nby + by) * nbx + bx;
+          short m = -1;
+          if (skip && dm.brick_empty[gi]) {
+            m = -2;
+          } else {
+            const int b3[3] = {bx, by, bz};
+            float lo[3], hi[3];
+            for (int a = 0; a < 3; ++a) {
+              const float sp = 1.f / dm.inv_spacing[a];
+              lo[a] = dm.origin[a] + sp * (float)(b3[a] * kBrickCells);
+              hi[a] = dm.origin[a] + sp * (float)min((b3[a] + 1) * kBrickCells, cmax[a] + 1);
+            }
+            if (staging && frustum_box(s_fr, T, s_t1, lo, hi)) {
+              const int slot = atomicAdd(&s_count, 1);
+              if (slot < kStageSlots) {
+                m = (short)slot;
+                s_list[slot] = (int)gi;
+              }
+            }
+          }
+          s_map[i] = m;
+        }
+        __syncthreads();
+        // too many frustum bricks for the slots: a shallower slab
+        if (s_count <= kStageSlots || s_level >= 5) break;
+        __syncthreads();
+        if (threadIdx.x == 0) s_level = s_level + 1;
+      }
+      const float t1s = s_t1;
+      const int staged = min(s_count, kStageSlots);
+
+      // stage the slab's bricks
+      if (staging && staged > 0) {
+        if (threadIdx.x == 0)
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&s_bar)),
+                       "r"((unsigned)(staged * kBrickFloats * 4))
+                       : "memory");
+        __syncthreads();
+        if (threadIdx.x < staged) {
+          const float *src = dm.bricks + (int64_t)s_list[threadIdx.x] * kBrickFloats;
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                  smem_addr(slots + threadIdx.x * kBrickFloats)),
+              "l"(src), "r"((unsigned)(kBrickFloats * 4)), "r"(smem_addr(&s_bar))
+              : "memory");
+        }
+        const bool ok = __syncthreads_and(stage_wait(&s_bar, phase, kStagePolls));
+        if (!ok) {
+          // give the copies a second, long bound to land, then stop staging:
+          // the rest of this CTA reads global memory (same values)
+          stage_wait(&s_bar, phase, kStagePolls * 8);
+          if (threadIdx.x == 0) atomicAdd(stage_fail, 1ull);
+          staging = false;
+        }
+        phase ^= 1u;
+      }
+      const bool use_map = staging;
+
+      // this slab's samples: t < min(bt1, slab end)
+      while (live) {
+        const float t = fmaf((float)k, dt, bt0);
+        if (!(t < bt1)) { live = false; break; }
+        if (!(t < t1s)) break;
+        ++k;
+        ++count;
+        int c[3];
+        float w[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float g = fmaf(t, B[a], A[a]);
+          c[a] = max(0, min((int)g, cmax[a]));
+          w[a] = g - (float)c[a];
+        }
+        const int bx = c[0] >> 3, by = c[1] >> 3, bz = c[2] >> 3;
+        const int loff = ((c[2] & 7) * kBrickNodes + (c[1] & 7)) * kBrickNodes + (c[0] & 7);
+        const int64_t gi = ((int64_t)bz * nby + by) * nbx + bx;
+        const int off = (int)(gi * kBrickFloats) + loff;
+        if (off != last_off) {
+          int m = -1;
+          if (use_map) {
+            const unsigned rx = (unsigned)(bx - s_box[0]), ry = (unsigned)(by - s_box[1]),
+                           rz = (unsigned)(bz - s_box[2]);
+            if (rx < (unsigned)s_box[3] && ry < (unsigned)s_box[4] && rz < (unsigned)s_box[5])
+              m = s_map[(rz * s_box[4] + ry) * s_box[3] + rx];
+          }
+          if (m == -2) continue;   // empty brick: zero opacity, counted
+          if (m >= 0) {
+            const float *q = slots + m * kBrickFloats + loff;
+            lc[0] = q[0];
+            lc[1] = q[1];
+            lc[2] = q[kBrickNodes];
+            lc[3] = q[kBrickNodes + 1];
+            lc[4] = q[kBrickNodes * kBrickNodes];
+            lc[5] = q[kBrickNodes * kBrickNodes + 1];
+            lc[6] = q[kBrickNodes * kBrickNodes + kBrickNodes];
+            lc[7] = q[kBrickNodes * kBrickNodes + kBrickNodes + 1];
+          } else {
+            const float *q = dm.bricks + off;
+            lc[0] = __ldg(q);
+            lc[1] = __ldg(q + 1);
+            lc[2] = __ldg(q + kBrickNodes);
+            lc[3] = __ldg(q + kBrickNodes + 1);
+            lc[4] = __ldg(q + kBrickNodes * kBrickNodes);
+            lc[5] = __ldg(q + kBrickNodes * kBrickNodes + 1);
+            lc[6] = __ldg(q + kBrickNodes * kBrickNodes + kBrickNodes);
+            lc[7] = __ldg(q + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+          }
+          last_off = off;
+        }
+        const float c00 = lerpf(lc[0], lc[1], w[0]);
+        const float c10 = lerpf(lc[2], lc[3], w[0]);
+        const float c01 = lerpf(lc[4], lc[5], w[0]);
+        const float c11 = lerpf(lc[6], lc[7], w[0]);
+        const float v = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
+        const float sc = __saturatef((v - mp.scalar_min) * mp.inv_range);
+        float4 col;
+        if (mp.lut_filter == GVR_LUT_LINEAR) {
+          col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, sc);
+        } else {
+          col = lut[min((int)(sc * nm1), mp.lut_size - 1)];
+        }
+        const float wa = (1.f - acc.w) * col.w;
+        acc.x = fmaf(wa, col.x, acc.x);
+        acc.y = fmaf(wa, col.y, acc.y);
+        acc.z = fmaf(wa, col.z, acc.z);
+        acc.w += wa;
+        if (acc.w >= thr) { live = false; break; }
+      }
+      __syncthreads();   // the slots and the map are rewritten by the next slab
+      if (threadIdx.x == 0) s_level = max(s_level - 1, 0);
+    }
+    // the domain's partial, as render_ray blends it
+    if (act && !(acc.w < mp.alpha_cull)) {
+      if (!have) {
+        crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
+        cdepth = bt1;
+        have = true;
+      } else if (ca < 1.f && acc.w != 0.f) {
+        const float op = 1.f - ca;
+        crgb[0] = fmaf(op, acc.x, crgb[0]);
+        crgb[1] = fmaf(op, acc.y, crgb[1]);
+        crgb[2] = fmaf(op, acc.z, crgb[2]);
+        ca = fminf(fmaf(op, acc.w, ca), 1.f);
+      }
+    }
+  }
+  if (valid) {
+    float4 out;
+    float dep;
+    finish_pixel(view, mp, px, py, have, crgb, ca, cdepth, out, dep);
+    const int64_t pix = (int64_t)py * mp.width + px;
+    rgba[pix] = out;
+    depth[pix] = dep;
+  }
+  if (samples) {
+    unsigned long long cnt = (unsigned long long)count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0 && cnt) atomicAdd(samples, cnt);
+  }
+}
+
+
 // Many views in one persistent launch. A device counter hands out work items
 // of `tiles_per_item` consecutive 16x16 tiles; items run through every tile
 // of view 0, then view 1, ... so neighbouring CTAs share bricks in L2. Each
@@ -724,7 +1190,8 @@ march_kernel(const DomainDev *__restrict__ g_domains, const ViewDev view,
 template <int PW, int UNROLL, int MINB, bool HEX>
 __global__ void __launch_bounds__(kThreads, MINB)
 batch_kernel(const DomainDev *__restrict__ g_domains, const ViewDev *__restrict__ views,
-             const int4 *__restrict__ rects, const MarchParams mp, int n_views, int tiles_x,
+             const int4 *__restrict__ rects, const __grid_constant__ MarchParams mp, int n_views,
+             int tiles_x,
              int tiles_y, int tiles_per_item, const float4 *__restrict__ g_lut,
              float4 *__restrict__ rgba, float *__restrict__ depth,
              unsigned long long *__restrict__ samples, unsigned int *__restrict__ queue)
@@ -850,6 +1317,42 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
   return cudaGetLastError();
 }
 
+
+namespace {
+
+using StagedFn = void (*)(const DomainDev *, const ViewDev, const MarchParams, const float4 *, float4 *,
+                          float *, unsigned long long *, const int *, const StageOrder,
+                          unsigned long long *);
+
+StagedFn select_staged(const Tuning &t)
+{
+  return t.packet_w == 4 ? staged_kernel<4> : (t.packet_w == 16 ? staged_kernel<16> : staged_kernel<8>);
+}
+
+size_t staged_smem(int lut_size, int n_domains)
+{
+  const size_t head = (sizeof(float4) * lut_size + sizeof(DomainDev) * n_domains + 127) & ~(size_t)127;
+  return head + sizeof(float) * kBrickFloats * kStageSlots;
+}
+
+}  // namespace
+
+cudaError_t launch_staged(const DomainDev *d_domains, const ViewDev &view, const MarchParams &mp,
+                          const float4 *d_lut, float4 *d_rgba, float *d_depth,
+                          unsigned long long *d_samples, const Tuning &tuning, const int *d_order,
+                          const StageOrder &order, unsigned long long *d_stage_fail,
+                          cudaStream_t stream)
+{
+  StagedFn fn = select_staged(tuning);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)staged_smem(kMaxLut, kMaxDomains));
+  if (e != cudaSuccess) return e;
+  const int64_t tiles = (int64_t)((mp.width + kTile - 1) / kTile) * ((mp.height + kTile - 1) / kTile);
+  fn<<<(unsigned)tiles, kThreads, staged_smem(mp.lut_size, mp.n_domains), stream>>>(
+      d_domains, view, mp, d_lut, d_rgba, d_depth, d_samples, d_order, order, d_stage_fail);
+  count_launch();
+  return cudaGetLastError();
+}
 
 namespace {
 

@@ -32,12 +32,22 @@ def _field_args(field):
 class Scene:
     """Domains resident on one CUDA device, rendered by the fused march kernel."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, brick_cells: int = 8):
+        """brick_cells: cells per brick axis (4, 8 or 16) of the vertex fields
+        this scene bricks (gvr_scene_set_brick_cells)."""
         h = C.c_void_p()
         N.call("gvr_scene_create", int(device), C.byref(h))
         self.handle = h
         self.device = int(device)
         self._hex_cells = {}
+        if brick_cells != 8:
+            self.set_brick_cells(brick_cells)
+        self.brick_cells = int(brick_cells)
+
+    def set_brick_cells(self, cells: int) -> None:
+        """Brick size of vertex fields added from now on (before any is added)."""
+        N.call("gvr_scene_set_brick_cells", self.handle, int(cells))
+        self.brick_cells = int(cells)
 
     def add_uniform(self, field, origin, spacing, association: int = N.ASSOC_VERTEX) -> int:
         """field shaped (nz, ny, nx) nodes (or cells for element association)."""
@@ -154,10 +164,18 @@ class Scene:
         N.call("gvr_scene_update_fields", self.handle, len(args), ids, ptrs, code, 1, loc, st)
         del args
 
-    def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4) -> None:
-        """Launch shape of the march kernel; images do not depend on it."""
+    def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4, staged: int = 0) -> None:
+        """Launch shape of the march kernel and whether the plain path stages
+        bricks in shared memory; images do not depend on either."""
         N.call("gvr_scene_set_tuning", self.handle, int(packet_w), int(unroll), int(min_blocks))
-        self.tuning = (int(packet_w), int(unroll), int(min_blocks))
+        N.call("gvr_scene_set_staging", self.handle, int(staged))
+        self.tuning = (int(packet_w), int(unroll), int(min_blocks), int(staged))
+
+    def staging_failures(self) -> int:
+        """Tiles whose bounded wait for staged bricks gave up (0 normally)."""
+        n = C.c_uint64(0)
+        N.call("gvr_scene_staging_failures", self.handle, C.byref(n))
+        return int(n.value)
 
     @property
     def num_domains(self) -> int:

@@ -3,7 +3,10 @@
 Candidates are the shapes gvr_scene_set_tuning accepts: pixel packet width
 per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1, 2,
 or 3 at 4 CTAs per SM) and the CTAs per SM the register budget targets (3
-or 4). Every candidate
+or 4), plus the shared-memory brick staging of gvr_scene_set_staging at
+each packet width; autotune_bricks also sweeps the brick size (4^3, 8^3 or
+16^3 cells, gvr_scene_set_brick_cells), building one scene per size. Every
+candidate
 renders the caller's own view on the caller's scene; the fastest median of
 a few CUDA-event-timed launches wins. Images do not depend on the shape, so
 tuning never changes results. Winners are cached per (GPU, workload key) in
@@ -23,7 +26,10 @@ from . import _native as N
 CANDIDATES = ([dict(packet_w=p, unroll=u, min_blocks=m)
                for p, u, m in itertools.product((8, 4, 16), (2, 1), (3, 4))] +
               [dict(packet_w=p, unroll=3, min_blocks=4) for p in (8, 4, 16)])
-# the batch kernel has no 3-sample variant (it would run as 2)
+# shared-memory brick staging (plain path, uniform vertex scenes; elsewhere
+# the scene runs the gather kernel of the same packet shape)
+STAGED_CANDIDATES = [dict(packet_w=p, unroll=1, min_blocks=3, staged=1) for p in (8, 4, 16)]
+# the batch kernel has no 3-sample variant (it would run as 2) and no staging
 BATCH_CANDIDATES = [c for c in CANDIDATES if c["unroll"] != 3]
 CACHE = Path(os.environ.get("GVR_TUNE_CACHE", Path.home() / ".cache" / "gvr_tune.json"))
 
@@ -87,9 +93,11 @@ def autotune_batch(scene, cameras, params, reps: int = 2) -> dict:
     return {"best": dict(best, tiles_per_item=g), "ms": {k: round(r[0], 4) for k, r in results.items()}}
 
 
-def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True) -> dict:
-    """Pick and set the fastest launch shape for this scene and view; returns
-    {"best": shape, "ms": {shape-string: median ms}, "cached": bool}."""
+def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True, staged: bool = True,
+             only_staged: bool = False) -> dict:
+    """Pick and set the fastest launch shape for this scene and view (with
+    staged=True also the shared-memory staging variant); returns {"best":
+    shape, "ms": {shape-string: median ms}, "cached": bool}."""
     import torch
     key = _key(scene, params)
     cache = {}
@@ -98,6 +106,7 @@ def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True) -> di
             cache = json.loads(CACHE.read_text())
         except Exception:
             cache = {}
+    key += "|staged" if only_staged else ("" if staged else "|gather")
     if use_cache and key in cache:
         best = cache[key]["best"]
         scene.set_tuning(**best)
@@ -107,10 +116,11 @@ def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True) -> di
     depth = torch.empty((params.height, params.width), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(scene.device)
     results = {}
-    for cand in CANDIDATES:
+    cands = STAGED_CANDIDATES if only_staged else CANDIDATES + (STAGED_CANDIDATES if staged else [])
+    for cand in cands:
         scene.set_tuning(**cand)
-        results[f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}"] = (
-            _time(scene, camera, params, rgba, depth, stream, reps), cand)
+        name = f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}" + ("s" if cand.get("staged") else "")
+        results[name] = (_time(scene, camera, params, rgba, depth, stream, reps), cand)
     name, (ms, best) = min(results.items(), key=lambda kv: kv[1][0])
     scene.set_tuning(**best)
     out = {"best": best, "ms": {k: round(v[0], 4) for k, v in results.items()}, "cached": False}
@@ -122,3 +132,29 @@ def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True) -> di
         except OSError:
             pass
     return out
+
+
+BRICK_CELLS = (4, 8, 16)
+
+
+def autotune_bricks(build_scene, camera, params, reps: int = 3, staged: bool = True) -> dict:
+    """Pick the brick size as well as the launch shape: build_scene(cells)
+    returns a Scene holding the workload bricked with `cells` cells per
+    brick axis; each is tuned with autotune() on this view. Returns {"best":
+    shape with "brick_cells", "ms": {brick size: {shape: ms}}, "scene": the
+    winning Scene (the others are closed)}. Images do not depend on the
+    brick size."""
+    results = {}
+    scenes = {}
+    for cells in BRICK_CELLS:
+        sc = build_scene(cells)
+        out = autotune(sc, camera, params, reps=reps, use_cache=False, staged=staged and cells == 8)
+        results[cells] = out
+        scenes[cells] = sc
+    best_cells = min(results, key=lambda c: min(results[c]["ms"].values()))
+    for c, sc in scenes.items():
+        if c != best_cells:
+            sc.close()
+    best = dict(results[best_cells]["best"], brick_cells=best_cells)
+    scenes[best_cells].set_tuning(**results[best_cells]["best"])
+    return {"best": best, "ms": {str(c): r["ms"] for c, r in results.items()}, "scene": scenes[best_cells]}

@@ -62,6 +62,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the ingest, plain-64, hex, batched, differentiable and compositing configurations")
+    ap.add_argument("--staging", choices=["auto", "off", "on"], default="auto",
+                    help="plain path: let the tuner choose between L1 gathers and shared-memory brick "
+                         "staging (auto), or time only one of them")
     return ap.parse_args()
 
 
@@ -133,14 +136,16 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def bricked_bytes(wl) -> int:
-    """Device bytes of the bricked fields: 736 floats per 8^3-cell brick."""
+def bricked_bytes(wl, cells: int = 8) -> int:
+    """Device bytes of the bricked fields: (cells + 1)^3 nodes per brick of
+    cells^3 cells, padded to a multiple of 32 floats (736 floats at 8)."""
+    floats = ((cells + 1) ** 3 + 31) // 32 * 32
     total = 0
     for d in wl.domains:
         nb = 1
         for n in d.dims:
-            nb *= (n - 1 + 7) // 8
-        total += nb * 736 * 4
+            nb *= (n - 1 + cells - 1) // cells
+        total += nb * floats * 4
     return total
 
 
@@ -173,8 +178,8 @@ def bench_config(wl, args) -> dict:
             "sample_dist_cells": 0.5, "early_term": 0.99,
             "lut": "1024-entry float LUT for both arms; the reference's multi-domain "
                    "uint8 LUT would round opacity to 0 below s=0.98 at 1774 samples",
-            "l2": f"inputs {bricked_bytes(wl) / 2**20:.0f} MiB bricked on the GPU (L2 129 MB); "
-                  "not flushed"}
+            "l2": f"field {sum(d.field.nbytes for d in wl.domains) / 2**20:.0f} MiB (more once "
+                  "bricked) against a 129 MB L2; not flushed"}
 
 
 def oracle_setup(wl, *, float_lut=False, camera=None):
@@ -690,15 +695,26 @@ def run_ours(args):
     cam = V.workload_camera(wl)
     params, _ = bench_params(wl)
     pixels = wl.width * wl.height
-    scene = S.Scene(dev)
-    V.load_workload(scene, wl)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
 
-    # launch shape for this scene and view (untimed), sample count of the
-    # view (deterministic), then warm-up
+    # brick size and launch shape for this scene and view (untimed): one
+    # scene per brick size, the fastest kept; then the sample count of the
+    # view (deterministic) and the warm-up
     from ascent_gb300 import tune
-    tuning = tune.autotune(scene, cam, params, use_cache=False)
+
+    def build_scene(cells):
+        sc = S.Scene(dev, brick_cells=cells)
+        V.load_workload(sc, wl)
+        return sc
+
+    if args.staging == "on":
+        scene = build_scene(8)
+        tuning = tune.autotune(scene, cam, params, use_cache=False, only_staged=True)
+        tuning["best"] = dict(tuning["best"], brick_cells=8)
+    else:
+        tuning = tune.autotune_bricks(build_scene, cam, params, staged=args.staging != "off")
+        scene = tuning.pop("scene")
     _, _, n_samples = scene.render(cam, params, device_out=True, stream=sptr, count_samples=True)
     for _ in range(max(args.warmup, 3)):
         scene.render(cam, params, device_out=True, stream=sptr)
@@ -764,7 +780,7 @@ def run_ours(args):
     # while the other renders, and neither waits for the other's blocking
     # publish. Every step still uploads its fields and reads its image back.
     import threading
-    scene2 = S.Scene(dev)
+    scene2 = S.Scene(dev, brick_cells=scene.brick_cells)
     V.load_workload(scene2, wl)
     scene2.set_tuning(*scene.tuning)
     pair = [scene, scene2]
@@ -820,7 +836,7 @@ def run_ours(args):
     achieved = alg_bytes / avg_launch_s / 1e9
     # informational: the bytes a launch cannot avoid (the bricked field read
     # once, the image written once) over the same time
-    compulsory = bricked_bytes(wl) + pixels * BYTES_PER_PIXEL
+    compulsory = bricked_bytes(wl, scene.brick_cells) + pixels * BYTES_PER_PIXEL
     traffic, traffic_wl = ncu_traffic(n_samples, pixels)
     value = replica_rate(world, n_samples, args.steps, total_ms / 1e3)
     e2e_value = replica_rate(world, n_samples, e2e_steps, e2e_s)

@@ -284,6 +284,29 @@ GVR_API int gvr_scene_num_domains(const gvr_scene *scene, int *n);
 GVR_API int gvr_scene_set_tuning(gvr_scene *scene, int packet_w, int unroll,
                                  int min_blocks);
 
+/* Brick size of the vertex fields this scene bricks from now on: 4, 8
+ * (default) or 16 cells per axis, so bricks of 5^3, 9^3 or 17^3 nodes
+ * (1.95x, 1.42x or 1.20x the field) and an empty-space map of that
+ * granularity. Call it before adding vertex-field domains (an error
+ * otherwise). Images do not depend on it. Set by the autotuner
+ * (ascent_gb300.tune.autotune_bricks); the reference keeps VTK-m's
+ * unbricked arrays, so no counterpart. */
+GVR_API int gvr_scene_set_brick_cells(gvr_scene *scene, int cells);
+
+/* How the plain march reads bricks: mode 0 gathers each sample's corners
+ * through the L1 cache; mode 1 stages, per 16 x 16 tile and slab of ray
+ * distance, the bricks the tile's rays cross into shared memory with bulk
+ * async copies and reads them there (scenes of uniform vertex-field domains
+ * in 8^3-cell bricks only; other scenes, and the batch path, use mode 0). Images are the same
+ * either way. Set by the autotuner (ascent_gb300.tune); the march the
+ * reference runs is VTK-m's (VolumeRenderer.cpp:258, 523-528), so no
+ * counterpart. */
+GVR_API int gvr_scene_set_staging(gvr_scene *scene, int mode);
+
+/* Number of tiles whose bounded wait for their staged bricks gave up since
+ * the scene was created (each finished from global memory; 0 normally). */
+GVR_API int gvr_scene_staging_failures(const gvr_scene *scene, uint64_t *n);
+
 /* Bounds {xmin,xmax,ymin,ymax,zmin,zmax} of one domain, or of the whole
  * scene when domain_id == -1 (DataSet::GetGlobalBounds). */
 GVR_API int gvr_scene_bounds(const gvr_scene *scene, int domain_id, double bounds[6]);

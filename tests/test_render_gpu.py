@@ -267,7 +267,7 @@ def test_every_launch_shape_gives_the_same_image():
     with S.Scene(0) as sc:
         V.load_workload(sc, wl)
         ref = None
-        for cand in tune.CANDIDATES:
+        for cand in tune.CANDIDATES + tune.STAGED_CANDIDATES:
             sc.set_tuning(**cand)
             g, gd, n = sc.render(cam, p, count_samples=True)
             if ref is None:
@@ -277,7 +277,8 @@ def test_every_launch_shape_gives_the_same_image():
             np.testing.assert_array_equal(gd, ref[1])
             assert n == ref[2]
         out = tune.autotune(sc, cam, p, reps=1, use_cache=False)
-        assert out["best"] in tune.CANDIDATES and len(out["ms"]) == len(tune.CANDIDATES)
+        every = tune.CANDIDATES + tune.STAGED_CANDIDATES
+        assert out["best"] in every and len(out["ms"]) == len(every)
         with pytest.raises(N.GvrError):
             sc.set_tuning(packet_w=5)
 
