@@ -198,6 +198,88 @@ __global__ void pixel_flag_kernel(const uint32_t *__restrict__ cnt, int64_t r,
   }
 }
 
+// The three pixel scans of the dense path in one pass over the counts:
+// off = exclusive scan of cnt (bucket offsets), upos / mpos = exclusive
+// scans of (cnt == 1) / (cnt > 1) (output slots). A tile of kTile3 pixels
+// per block writes its local prefixes and its totals; one block scans the
+// tile totals (at most kTile3 tiles, so r <= kTile3^2); a last pass adds
+// each tile's base. Replaces a copy, a flag kernel and three three-launch
+// scans (11 operations) by three launches.
+constexpr int kTile3 = 1024;
+
+__device__ __forceinline__ uint3 add3(uint3 a, uint3 b) { return make_uint3(a.x + b.x, a.y + b.y, a.z + b.z); }
+
+// Inclusive block scan of one uint3 per thread (kTile3 threads); returns the
+// thread's inclusive prefix, *tot receives the block total.
+__device__ __forceinline__ uint3 block_scan3(uint3 v, uint3 *tot)
+{
+  __shared__ uint3 warp_tot[kTile3 / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint3 x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint3 y;
+    y.x = __shfl_up_sync(0xffffffffu, x.x, o);
+    y.y = __shfl_up_sync(0xffffffffu, x.y, o);
+    y.z = __shfl_up_sync(0xffffffffu, x.z, o);
+    if (lane >= o) x = add3(x, y);
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint3 t = warp_tot[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      uint3 y;
+      y.x = __shfl_up_sync(0xffffffffu, t.x, o);
+      y.y = __shfl_up_sync(0xffffffffu, t.y, o);
+      y.z = __shfl_up_sync(0xffffffffu, t.z, o);
+      if (lane >= o) t = add3(t, y);
+    }
+    warp_tot[lane] = t;
+  }
+  __syncthreads();
+  if (warp > 0) x = add3(x, warp_tot[warp - 1]);
+  *tot = warp_tot[kTile3 / 32 - 1];
+  return x;
+}
+
+__global__ void __launch_bounds__(kTile3)
+scan3_tile_kernel(const uint32_t *__restrict__ cnt, int64_t r, uint32_t *__restrict__ off,
+                  uint32_t *__restrict__ upos, uint32_t *__restrict__ mpos, uint3 *__restrict__ sums)
+{
+  const int64_t p = (int64_t)blockIdx.x * kTile3 + threadIdx.x;
+  const uint32_t c = p < r ? cnt[p] : 0u;
+  const uint3 v = make_uint3(c, c == 1, c > 1);
+  uint3 tot;
+  const uint3 inc = block_scan3(v, &tot);
+  if (p < r) {
+    off[p] = inc.x - v.x;
+    upos[p] = inc.y - v.y;
+    mpos[p] = inc.z - v.z;
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+// One block: exclusive scan of the tile totals in place.
+__global__ void __launch_bounds__(kTile3) scan3_top_kernel(uint3 *__restrict__ sums, int tiles)
+{
+  const uint3 v = threadIdx.x < tiles ? sums[threadIdx.x] : make_uint3(0u, 0u, 0u);
+  uint3 tot;
+  const uint3 inc = block_scan3(v, &tot);
+  if (threadIdx.x < tiles) sums[threadIdx.x] = make_uint3(inc.x - v.x, inc.y - v.y, inc.z - v.z);
+}
+
+__global__ void __launch_bounds__(kTile3)
+scan3_add_kernel(int64_t r, uint32_t *__restrict__ off, uint32_t *__restrict__ upos,
+                 uint32_t *__restrict__ mpos, const uint3 *__restrict__ sums)
+{
+  const int64_t p = (int64_t)blockIdx.x * kTile3 + threadIdx.x;
+  if (p >= r) return;
+  const uint3 b = sums[blockIdx.x];
+  off[p] += b.x;
+  upos[p] += b.y;
+  mpos[p] += b.z;
+}
+
 constexpr int kLocalSort = 32;  // records per pixel ordered in thread-local arrays
 
 __device__ __forceinline__ bool before(uint32_t ka, uint32_t ia, uint32_t kb, uint32_t ib)
@@ -285,7 +367,8 @@ struct Arena {
 
 size_t dense_bytes(int64_t n, int64_t r)
 {
-  return 256 * 9 + (4 * (size_t)r + 2 * (size_t)n + scan_scratch_words(r) + 3) * sizeof(uint32_t);
+  return 256 * 9 + (4 * (size_t)r + 2 * (size_t)n + std::max<size_t>(scan_scratch_words(r), 3 * 1024) + 3) *
+                       sizeof(uint32_t);
 }
 
 size_t sorted_bytes(int64_t n)
@@ -301,19 +384,32 @@ cudaError_t composite_dense(const Partial *in, int64_t n, int lo, int64_t r, Par
   uint32_t *cnt = a.take<uint32_t>(r), *off = a.take<uint32_t>(r);
   uint32_t *upos = a.take<uint32_t>(r), *mpos = a.take<uint32_t>(r);
   uint32_t *rank = a.take<uint32_t>(n), *order = a.take<uint32_t>(n);
-  uint32_t *scan_tmp = a.take<uint32_t>(scan_scratch_words(r));
+  uint32_t *scan_tmp = a.take<uint32_t>(std::max<size_t>(scan_scratch_words(r), 3 * (size_t)kTile3));
   cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * r, st);
   if (e != cudaSuccess) return e;
   count_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, cnt, rank, bad);
   count_launch();
-  if ((e = cudaMemcpyAsync(off, cnt, sizeof(uint32_t) * r, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-  if ((e = exclusive_scan(off, r, scan_tmp, st)) != cudaSuccess) return e;
+  const int64_t tiles = (r + kTile3 - 1) / kTile3;
+  if (tiles <= kTile3) {
+    uint3 *sums = reinterpret_cast<uint3 *>(scan_tmp);   // 3 words per tile, within scan_tmp
+    scan3_tile_kernel<<<(unsigned)tiles, kTile3, 0, st>>>(cnt, r, off, upos, mpos, sums);
+    count_launch();
+    if (tiles > 1) {
+      scan3_top_kernel<<<1, kTile3, 0, st>>>(sums, (int)tiles);
+      scan3_add_kernel<<<(unsigned)tiles, kTile3, 0, st>>>(r, off, upos, mpos, sums);
+      count_launch(2);
+    }
+  } else {
+    if ((e = cudaMemcpyAsync(off, cnt, sizeof(uint32_t) * r, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+      return e;
+    if ((e = exclusive_scan(off, r, scan_tmp, st)) != cudaSuccess) return e;
+    pixel_flag_kernel<<<grid_of(r), 256, 0, st>>>(cnt, r, upos, mpos);
+    count_launch();
+    if ((e = exclusive_scan(upos, r, scan_tmp, st)) != cudaSuccess) return e;
+    if ((e = exclusive_scan(mpos, r, scan_tmp, st)) != cudaSuccess) return e;
+  }
   bucket_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, off, rank, order);
   count_launch();
-  pixel_flag_kernel<<<grid_of(r), 256, 0, st>>>(cnt, r, upos, mpos);
-  count_launch();
-  if ((e = exclusive_scan(upos, r, scan_tmp, st)) != cudaSuccess) return e;
-  if ((e = exclusive_scan(mpos, r, scan_tmp, st)) != cudaSuccess) return e;
   pixel_emit_kernel<<<grid_of(r), 256, 0, st>>>(in, cnt, off, upos, mpos, order, r, out, totals);
   count_launch();
   return cudaGetLastError();

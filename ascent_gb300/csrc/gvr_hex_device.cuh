@@ -39,8 +39,14 @@ constexpr float kHexNewtonTol = 2e-3f;     // |step|_inf in reference space
 // accepted when the solution lies at least kHexLooseMargin inside every
 // face; near a face, where such an error could decide which cell holds the
 // sample, the solve goes on to kHexNewtonTol.
-constexpr float kHexLooseTol = 0.05f;
-constexpr float kHexLooseMargin = 0.01f;
+#ifndef GVR_HEX_LOOSE_TOL
+#define GVR_HEX_LOOSE_TOL 0.05f
+#endif
+#ifndef GVR_HEX_LOOSE_MARGIN
+#define GVR_HEX_LOOSE_MARGIN 0.01f
+#endif
+constexpr float kHexLooseTol = GVR_HEX_LOOSE_TOL;
+constexpr float kHexLooseMargin = GVR_HEX_LOOSE_MARGIN;
 constexpr float kHexInsideTol = 2e-4f;     // r, s, t in [-tol, 1 + tol]
 constexpr int kHexStack = 64;
 constexpr int kHexHops = 4;                // face-neighbour steps before the LBVH walk

@@ -62,6 +62,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the ingest, plain-64, hex, batched, differentiable and compositing configurations")
+    ap.add_argument("--configs", default="",
+                    help="comma-separated subset of ingest,plain_64,hex,batched,differentiable,composite "
+                         "(default: all)")
     ap.add_argument("--staging", choices=["auto", "off", "on"], default="auto",
                     help="plain path: let the tuner choose between L1 gathers and shared-memory brick "
                          "staging (auto), or time only one of them")
@@ -851,12 +854,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         ocam, oparams = oracle_setup(wl, float_lut=True)
         main_acc = accuracy(dev, wl, [cam], params, [ocam], oparams)
-        others["ingest"] = bench_ingest(dev, wl)
-        others["plain_64"] = bench_plain_small(dev)
-        others["hex"] = bench_hex(dev)
-        others["batched"] = bench_batch(dev)
-        others["differentiable"] = bench_diff(dev)
-        others["composite"] = bench_composite(dev)
+        runs = {"ingest": lambda: bench_ingest(dev, wl), "plain_64": lambda: bench_plain_small(dev),
+                "hex": lambda: bench_hex(dev), "batched": lambda: bench_batch(dev),
+                "differentiable": lambda: bench_diff(dev), "composite": lambda: bench_composite(dev)}
+        for name in (args.configs.split(",") if args.configs else runs):
+            others[name] = runs[name]()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

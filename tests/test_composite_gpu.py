@@ -147,3 +147,22 @@ def test_async_caller_range_flags_records_outside(comp):
     empty = torch.zeros((0, 6), dtype=torch.int32, device="cuda")
     _, n0 = comp.composite_partials_device_async(empty, 0, 10)
     assert int(n0.item()) == 0
+
+
+def test_dense_path_beyond_one_scan_tile_of_tiles(comp):
+    """Pixel ranges above 1024^2 take the three separate scans instead of
+    the fused one; both orders and blends equal the restatement."""
+    rng = np.random.default_rng(40)
+    n = 1_300_000
+    p = np.zeros(n, comp.PARTIAL_DTYPE)
+    p["pixel_id"] = rng.integers(0, 2_200_000, n)
+    p["depth"] = rng.uniform(0, 4, n).astype(np.float32)
+    a = rng.uniform(0.01, 1, n).astype(np.float32)
+    p["alpha"] = a
+    p["rgb"] = (rng.uniform(0, 1, (n, 3)) * a[:, None]).astype(np.float32)
+    ims = [p[: n // 2], p[n // 2:]]
+    ref = O.composite_partials_f32(ims)
+    assert comp.PartialCompositor().composite(ims).tobytes() == ref.tobytes()
+    d = comp.to_device(p)
+    out, n_out = comp.composite_partials_device_async(d, 0, 2_200_000 - 1)
+    assert comp.from_device(out[: int(n_out.item())]).tobytes() == ref.tobytes()
