@@ -5,6 +5,7 @@
 // distance, transfer-function sampling, cameras, visibility order, domain
 // bookkeeping) plus the orchestration of the device kernels.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -723,7 +724,39 @@ int gvr_scene_update_fields(gvr_scene *s, int n, const int *domain_ids, const vo
   std::vector<const float2 *> job_ranges;
   std::vector<int64_t> job_bricks;
   std::vector<float2 *> job_out;
-  for (int k = 0; k < n; ++k) {
+  // device-resident contiguous float32 fields in 8^3-cell bricks: every
+  // field's bricking in one launch, so that the domains' tails overlap
+  bool merged = location == GVR_MEM_DEVICE && dtype == GVR_DTYPE_FLOAT32 && stride == 1;
+  for (int k = 0; k < n && merged; ++k) {
+    const Domain &d = s->domains[domain_ids[k]];
+    if (piped(d) && d.dev.bshift != kBrickShiftDefault) merged = false;
+  }
+  if (merged) {
+    std::vector<const float *> srcs;
+    std::vector<float *> bricks;
+    std::vector<float2 *> ranges;
+    std::vector<std::array<int, 3>> dims, nbrick;
+    for (int k = 0; k < n; ++k) {
+      Domain &d = s->domains[domain_ids[k]];
+      if (!piped(d)) continue;
+      srcs.push_back(static_cast<const float *>(fields[k]));
+      bricks.push_back(d.d_bricks);
+      ranges.push_back(d.d_brick_range);
+      dims.push_back({d.dev.dims[0], d.dev.dims[1], d.dev.dims[2]});
+      nbrick.push_back({d.dev.nbrick[0], d.dev.nbrick[1], d.dev.nbrick[2]});
+      job_ranges.push_back(d.d_brick_range);
+      job_bricks.push_back(d.n_bricks);
+      job_out.push_back(s->d_ranges + k);
+      ++j;
+    }
+    if (j > 0) {
+      e = launch_brick_device_many(j, srcs.data(), reinterpret_cast<const int(*)[3]>(dims.data()),
+                                   bricks.data(), reinterpret_cast<const int(*)[3]>(nbrick.data()),
+                                   ranges.data(), d_timed_out, st);
+      if (e != cudaSuccess) return cuda_error(e, "field bricking");
+    }
+  }
+  for (int k = 0; k < n && !merged; ++k) {
     Domain &d = s->domains[domain_ids[k]];
     if (!piped(d)) continue;
     const void *dsrc = fields[k];

@@ -7,6 +7,7 @@
 // renderer's own: 8^3-cell bricks with a one-node apron plus a per-brick
 // {min,max} macrocell grid used for empty-space skipping.
 #include <cstdlib>
+#include <cstring>
 #include <cfloat>
 #include <cstdint>
 #include <cstdio>
@@ -122,16 +123,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(const uint64_t *bar, long long
   return false;
 }
 
-__global__ void __launch_bounds__(256)
-brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny, int nz, int nbx,
-                    int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range,
-                    int *__restrict__ timed_out, long long first_polls)
+// One run of up to 16 bricks of one field (the body of both launches below).
+__device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t n_src, int nx, int ny,
+                                          int nz, int nbx, int nby, int run, int by, int bz,
+                                          float *__restrict__ bricks, float2 *__restrict__ brick_range,
+                                          int *__restrict__ timed_out, long long first_polls)
 {
   __shared__ __align__(16) float rows[kRows * kRowSlot];
   __shared__ int lead[kRows];
   __shared__ int plain[kRows];
   __shared__ __align__(8) uint64_t bar;
-  const int run = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
   const int x0 = run * kRunBricks * kBrickCells;
   const int count = min(kRunNodes, nx - x0);
   const uintptr_t base = reinterpret_cast<uintptr_t>(src);
@@ -222,6 +223,47 @@ brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny
     }
     if (lane == 0) brick_range[b] = bad ? make_float2(NAN, NAN) : make_float2(vmin, vmax);
   }
+}
+
+__global__ void __launch_bounds__(256)
+brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny, int nz, int nbx,
+                    int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range,
+                    int *__restrict__ timed_out, long long first_polls)
+{
+  brick_run(src, n_src, nx, ny, nz, nbx, nby, blockIdx.x, blockIdx.y, blockIdx.z, bricks, brick_range,
+            timed_out, first_polls);
+}
+
+// Many fields in one launch (a device-resident publish): block b belongs to
+// the job whose [first, first of the next) block range holds it and runs
+// that field's run (b - first) % runs, row by, layer bz. One launch instead
+// of one per domain lets the domains' tails overlap.
+struct StagedJobs {
+  const float *src[kMaxDomains];
+  float *bricks[kMaxDomains];
+  float2 *brick_range[kMaxDomains];
+  int64_t n_src[kMaxDomains];
+  int dims[kMaxDomains][3];
+  int nbrick[kMaxDomains][3];
+  int runs[kMaxDomains];
+  int first[kMaxDomains + 1];   // first block of each job; first[n] = total
+  int n;
+};
+
+__global__ void __launch_bounds__(256)
+brick_staged_multi_kernel(const __grid_constant__ StagedJobs jobs, int *__restrict__ timed_out,
+                          long long first_polls)
+{
+  const int b = blockIdx.x;
+  int j = 0;
+  while (j + 1 < jobs.n && b >= jobs.first[j + 1]) ++j;
+  const int local = b - jobs.first[j];
+  const int run = local % jobs.runs[j];
+  const int by = (local / jobs.runs[j]) % jobs.nbrick[j][1];
+  const int bz = local / (jobs.runs[j] * jobs.nbrick[j][1]);
+  brick_run(jobs.src[j], jobs.n_src[j], jobs.dims[j][0], jobs.dims[j][1], jobs.dims[j][2],
+            jobs.nbrick[j][0], jobs.nbrick[j][1], run, by, bz, jobs.bricks[j], jobs.brick_range[j],
+            timed_out, first_polls);
 }
 
 }  // namespace
@@ -439,6 +481,35 @@ __global__ void __launch_bounds__(1024) range_of_bricks_kernel(const RangeJobs j
 }
 
 }  // namespace
+
+cudaError_t launch_brick_device_many(int n, const float *const *srcs, const int (*dims)[3],
+                                     float *const *bricks, const int (*nbrick)[3],
+                                     float2 *const *brick_range, int *d_timed_out, cudaStream_t stream)
+{
+  if (n < 1 || n > kMaxDomains) return cudaErrorInvalidValue;
+  StagedJobs jobs;
+  std::memset(static_cast<void *>(&jobs), 0, sizeof(jobs));
+  jobs.n = n;
+  int64_t total = 0;
+  for (int j = 0; j < n; ++j) {
+    jobs.src[j] = srcs[j];
+    jobs.bricks[j] = bricks[j];
+    jobs.brick_range[j] = brick_range[j];
+    jobs.n_src[j] = (int64_t)dims[j][0] * dims[j][1] * dims[j][2];
+    for (int a = 0; a < 3; ++a) {
+      jobs.dims[j][a] = dims[j][a];
+      jobs.nbrick[j][a] = nbrick[j][a];
+    }
+    jobs.runs[j] = (nbrick[j][0] + kRunBricks - 1) / kRunBricks;
+    jobs.first[j] = (int)total;
+    total += (int64_t)jobs.runs[j] * nbrick[j][1] * nbrick[j][2];
+    if (total >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+  }
+  jobs.first[n] = (int)total;
+  brick_staged_multi_kernel<<<(unsigned)total, 256, 0, stream>>>(jobs, d_timed_out, stage_first_polls());
+  count_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                                 int bshift, float *d_bricks, const int nbrick[3],

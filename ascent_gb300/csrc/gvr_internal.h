@@ -250,6 +250,12 @@ cudaError_t launch_brick_field(const void *src, int dtype, int64_t stride,
 cudaError_t launch_brick_device(const void *dsrc, int dtype, int64_t stride, const int dims[3],
                                 int bshift, float *d_bricks, const int nbrick[3],
                                 float2 *d_brick_range, int *d_timed_out, cudaStream_t stream);
+// Brick n contiguous float32 fields in device memory into 8^3-cell bricks in
+// one launch (the staged kernel's runs of all fields), with per-brick
+// ranges; a staged copy that gives up waiting sets *d_timed_out.
+cudaError_t launch_brick_device_many(int n, const float *const *srcs, const int (*dims)[3],
+                                     float *const *bricks, const int (*nbrick)[3],
+                                     float2 *const *brick_range, int *d_timed_out, cudaStream_t stream);
 // Reduce n domains' per-brick ranges to one range each (*out[j]; NaN when a
 // brick holds a non-finite value): one launch, one block per domain.
 cudaError_t launch_ranges_of_bricks(int n, const float2 *const *brick_ranges,

@@ -40,7 +40,18 @@ def test_staged_wait_timeout_reports_and_recovers(monkeypatch):
         assert err.value.code == N.GVR_ERR_TIMEOUT
         assert np.isnan(sc.scalar_range()).all()
 
+        # device-resident fields: all domains bricked by one launch
+        import torch
+        dev_fields = [torch.from_numpy(f).cuda() for f in fields]
+        with pytest.raises(N.GvrError) as err:
+            sc.update_fields([0, 1], dev_fields)
+        assert err.value.code == N.GVR_ERR_TIMEOUT
+        assert np.isnan(sc.scalar_range()).all()
+
         monkeypatch.delenv("GVR_STAGE_WAIT_POLLS")
+        sc.update_fields([0, 1], dev_fields)
+        np.testing.assert_array_equal(sc.scalar_range(), good_range)
+        np.testing.assert_array_equal(sc.render(cam, p)[0], before)
         sc.update_fields([0, 1], fields)
         np.testing.assert_array_equal(sc.scalar_range(), good_range)
         after, after_d = sc.render(cam, p)

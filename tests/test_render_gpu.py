@@ -353,6 +353,11 @@ def test_update_fields_pipelined_equals_one_by_one():
         sc.add_hex(h.x, h.y, h.z, h.conn, h.field)
         sc.update_fields([0, 1], [new[0], (h.field * 2).astype(np.float32)])
         assert sc.scalar_range()[1] >= float((h.field * 2).max()) - 1e-6
+        # the same from device memory: the uniform domain takes the one-launch
+        # bricking, the hex domain its own path
+        sc.update_fields([0, 1], [torch.from_numpy(new[0]).cuda(),
+                                  torch.from_numpy((h.field * 3).astype(np.float32)).cuda()])
+        assert sc.scalar_range()[1] >= float((h.field * 3).max()) - 1e-6
 
 
 @pytest.mark.parametrize("name", ["Viridis", "Jet", "black-body radiation"])
