@@ -309,7 +309,42 @@ __global__ void pixel_emit_kernel(const Partial *__restrict__ in, const uint32_t
       continue;
     }
     Partial res;
-    if (c <= kLocalSort) {
+    if (c <= 8) {
+      // the common case (one record per partial image, at most 8 images):
+      // keys and indices in registers, ordered by Batcher's odd-even merge
+      // network for 8 inputs (19 compare-exchanges; padding sorts last)
+      uint32_t key[8], idx[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if ((uint32_t)j < c) {
+          const uint32_t i = seg[j];
+          key[j] = order_bits(in[i].depth);
+          idx[j] = i;
+        } else {
+          key[j] = 0xffffffffu;
+          idx[j] = 0xffffffffu;
+        }
+      }
+      auto cx = [&](int a, int b) {
+        if (before(key[b], idx[b], key[a], idx[a])) {
+          const uint32_t tk = key[a], ti = idx[a];
+          key[a] = key[b];
+          idx[a] = idx[b];
+          key[b] = tk;
+          idx[b] = ti;
+        }
+      };
+      cx(0, 1); cx(2, 3); cx(4, 5); cx(6, 7);
+      cx(0, 2); cx(1, 3); cx(4, 6); cx(5, 7);
+      cx(1, 2); cx(5, 6);
+      cx(0, 4); cx(1, 5); cx(2, 6); cx(3, 7);
+      cx(2, 4); cx(3, 5);
+      cx(1, 2); cx(3, 4); cx(5, 6);
+      res = in[idx[0]];
+#pragma unroll
+      for (int j = 1; j < 8; ++j)
+        if ((uint32_t)j < c) blend_into(res, in[idx[j]]);
+    } else if (c <= kLocalSort) {
       uint32_t key[kLocalSort], idx[kLocalSort];
       for (uint32_t j = 0; j < c; ++j) {
         const uint32_t i = seg[j];

@@ -307,6 +307,8 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
     stream = torch.cuda.current_stream(dev)
     rgba = torch.empty((size, size, 4), dtype=torch.float32, device=f"cuda:{dev}")
     depth = torch.empty((size, size), dtype=torch.float32, device=f"cuda:{dev}")
+    from ascent_gb300 import tune
+    tuning = tune.autotune(sc, cam, p, reps=2, use_cache=False, staged=False)
     _, _, n = sc.render(cam, p, device_out=True, count_samples=True)
     args = (sc.handle, C.byref(cam), C.byref(p), C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()),
             N.MEM_DEVICE, C.c_void_p(stream.cuda_stream), None)
@@ -326,6 +328,7 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
             "cpu_port_gsamples_per_s": cpu["value"], "cpu_cores": cpu["cores"],
             "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
             "bvh_build_ms": build_ms, "face_neighbour_build_ms": nbr_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
+            "tuning": tuning["best"],
             "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": pk["hbm_gbs"],
                          "unit": "GB/s", "frac": alg / ms / 1e6 / pk["hbm_gbs"],
                          "bytes_per_sample": 160}}
@@ -593,6 +596,8 @@ def bench_plain_small(dev, reps=20) -> dict:
         V.load_workload(sc, wl)
         rgba = torch.empty((512, 512, 4), dtype=torch.float32, device=f"cuda:{dev}")
         depth = torch.empty((512, 512), dtype=torch.float32, device=f"cuda:{dev}")
+        from ascent_gb300 import tune
+        tuning = tune.autotune(sc, cam, p, reps=3, use_cache=False)
         _, _, n = sc.render(cam, p, device_out=True, count_samples=True)
         args = (sc.handle, C.byref(cam), C.byref(p), C.c_void_p(rgba.data_ptr()),
                 C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, C.c_void_p(stream.cuda_stream), None)
@@ -602,7 +607,8 @@ def bench_plain_small(dev, reps=20) -> dict:
     cpu = cpu_sample(wl, 3.0)
     ocam, op = oracle_setup(wl)
     return {"workload": wl.name, "samples_per_frame": n, "gsamples_per_s": n / ms / 1e6,
-            "fps": 1e3 / ms, "ms_per_frame": ms, "cpu_port_gsamples_per_s": cpu["value"],
+            "fps": 1e3 / ms, "ms_per_frame": ms, "tuning": tuning["best"],
+            "cpu_port_gsamples_per_s": cpu["value"],
             "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
             "error_vs_fp64_oracle": accuracy(dev, wl, [cam], p, [ocam], op)}
 
