@@ -157,3 +157,25 @@ def test_scratch_trim_arguments():
     with pytest.raises(N.GvrError):
         N.scratch_trim(-1, 0)
     assert N.scratch_trim(63, 0) == 0
+
+
+@pytest.mark.parametrize("parts", [None, (2, 1, 2)])
+def test_oracle_setup_equals_library_setup(parts):
+    """The oracle builds the camera and render parameters of a workload with
+    its own functions (no product library); on the same workload they equal
+    the library's field for field, LUT included (float on the one-domain
+    path, through uint8 on the multi-domain path)."""
+    from ascent_gb300 import volume as V
+    from ascent_gb300 import workloads as W
+    wl = W.plain_small(n=24, width=40, height=30, parts=parts)
+    assert bytes(O.workload_camera(wl)) == bytes(V.workload_camera(wl))
+    op, pp = O.workload_params(wl), V.workload_params(wl)
+    for f in ("width", "height", "sample_dist", "scalar_min", "scalar_max", "lut_size", "lut_filter",
+              "alpha_cull", "early_term", "quantize_uint8", "render_bg", "clear_depth"):
+        assert getattr(op, f) == getattr(pp, f), f
+    n = op.lut_size * 4
+    np.testing.assert_array_equal(np.ctypeslib.as_array(op.lut_rgba, (n,)),
+                                  np.ctypeslib.as_array(pp.lut_rgba, (n,)))
+    angles = W.cinema_angles(3, 2)
+    assert [bytes(c) for c in O.cinema_cameras(wl.bounds, angles)] == \
+           [bytes(c) for c in S.cinema_cameras(wl.bounds, angles)]
