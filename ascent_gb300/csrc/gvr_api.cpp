@@ -832,11 +832,12 @@ int gvr_scene_set_batch_granularity(gvr_scene *s, int tiles_per_item)
 int gvr_scene_set_tuning(gvr_scene *s, int packet_w, int unroll, int min_blocks)
 {
   if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
-  if ((packet_w != 4 && packet_w != 8 && packet_w != 16) || unroll < 1 || unroll > 3 ||
-      (min_blocks != 3 && min_blocks != 4) || (unroll == 3 && min_blocks != 4))
+  if ((packet_w != 4 && packet_w != 8 && packet_w != 16) || unroll < 1 || unroll > 4 ||
+      (min_blocks != 3 && min_blocks != 4) || (unroll == 4 && packet_w == 16) ||
+      (unroll == 3 && min_blocks == 3 && packet_w == 16))
     return set_error(GVR_ERR_INVALID_ARGUMENT,
-                     "tuning: packet_w in {4,8,16}, unroll in {1,2,3}, min_blocks in {3,4}; "
-                     "unroll 3 needs min_blocks 4");
+                     "tuning: packet_w in {4,8,16}, unroll in {1,2,3,4}, min_blocks in {3,4}; "
+                     "16-wide packets take at most 3 samples per iteration, and 3 only at 4 CTAs per SM");
   s->tuning.packet_w = packet_w;
   s->tuning.unroll = unroll;
   s->tuning.min_blocks = min_blocks;

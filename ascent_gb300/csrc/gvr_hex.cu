@@ -258,7 +258,7 @@ __global__ void locate_kernel(const DomainDev dm, const float *__restrict__ pts,
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
     float rst[3];
-    float4 v[8];
+    HexGeom v;
     const int c = hex_locate(dm, p, rst, v);
     cells[i] = c;
     rst_out[3 * i] = rst[0];
@@ -304,7 +304,8 @@ __global__ void node_range_kernel(const float4 *__restrict__ nodes, int64_t n, f
 }
 
 // Monomial coefficients of every cell's trilinear map (position and vertex
-// field), 8 float4 per cell, from its corner nodes (see hex_load).
+// field) from its corner nodes: 32 floats per cell, c0.xyz .. c7.xyz then
+// w0 .. w7 (see hex_load).
 __global__ void coef_kernel(const float4 *__restrict__ nodes, const int4 *__restrict__ conn,
                             int64_t n_cells, float4 *__restrict__ coef)
 {
@@ -328,12 +329,16 @@ __global__ void coef_kernel(const float4 *__restrict__ nodes, const int4 *__rest
                            {-1, 0, 0, 1, 0, 0, 0, 0},  {-1, 0, 0, 0, 1, 0, 0, 0},
                            {1, -1, 1, -1, 0, 0, 0, 0}, {1, -1, 0, 0, -1, 1, 0, 0},
                            {1, 0, 0, -1, -1, 0, 0, 1}, {-1, 1, -1, 1, 1, -1, 1, -1}};
+    float f[32];
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-      o[k] = make_float4(comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::x),
-                         comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::y),
-                         comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::z),
-                         comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::w));
+    for (int k = 0; k < 8; ++k) {
+      f[3 * k] = comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::x);
+      f[3 * k + 1] = comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::y);
+      f[3 * k + 2] = comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::z);
+      f[24 + k] = comb(w[k][0], w[k][1], w[k][2], w[k][3], w[k][4], w[k][5], w[k][6], w[k][7], &float4::w);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
   }
 }
 

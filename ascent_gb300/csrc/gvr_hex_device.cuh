@@ -54,27 +54,50 @@ constexpr int kHexHops = 4;                // face-neighbour steps before the LB
 constexpr float kHexPredictMargin = 0.02f; // guess this far outside: step before solving
 
 // A cell's trilinear map x(r,s,t) = sum_k c_k m_k(r,s,t) over the monomials
-// m = (1, r, s, t, rs, rt, st, rst); c_k.xyz are position coefficients and
-// c_k.w those of the vertex field. From the VTK corners v0..v7:
+// m = (1, r, s, t, rs, rt, st, rst); c_k are position coefficients and w_k
+// those of the vertex field. From the VTK corners v0..v7:
 //   c0 = v0, c1 = v1 - v0, c2 = v3 - v0, c3 = v4 - v0,
 //   c4 = v2 - v1 - v3 + v0, c5 = v5 - v1 - v4 + v0, c6 = v7 - v3 - v4 + v0,
 //   c7 = v6 - v2 - v5 - v7 + v1 + v3 + v4 - v0.
 // Evaluating the map and its Jacobian this way takes ~50 multiply-adds per
-// Newton step instead of ~140 through the corner weights, and a cell's
-// eight records are 128 contiguous bytes.
-__device__ __forceinline__ void hex_load(const DomainDev &dm, int cell, float4 (&v)[8])
+// Newton step instead of ~140 through the corner weights. A cell's record
+// is 32 contiguous floats (8 float4, 128 bytes): the 24 position
+// coefficients c0.xyz .. c7.xyz, then w0 .. w7. The march keeps the 24
+// position coefficients in registers while it stays in a cell and reads the
+// field's 8 (two float4, usually L1 hits) only to interpolate a sample, so
+// the Newton solve has 8 more registers than with whole float4 corners.
+struct HexGeom {
+  float c[8][3];
+};
+
+__device__ __forceinline__ void hex_load(const DomainDev &dm, int cell, HexGeom &g)
 {
-  const float4 *c = dm.hex_coef + 8 * (int64_t)cell;
+  const float4 *q = dm.hex_coef + 8 * (int64_t)cell;
+  float f[24];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = __ldg(c + k);
+  for (int k = 0; k < 6; ++k) {
+    const float4 a = __ldg(q + k);
+    f[4 * k] = a.x;
+    f[4 * k + 1] = a.y;
+    f[4 * k + 2] = a.z;
+    f[4 * k + 3] = a.w;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    g.c[k][0] = f[3 * k];
+    g.c[k][1] = f[3 * k + 1];
+    g.c[k][2] = f[3 * k + 2];
+  }
 }
 
-// Value of the vertex field at (r, s, t) from the coefficients' w.
-__device__ __forceinline__ float hex_value(const float4 (&c)[8], float r, float s, float t)
+// Value of the vertex field of cell `cell` at (r, s, t).
+__device__ __forceinline__ float hex_value(const DomainDev &dm, int cell, float r, float s, float t)
 {
+  const float4 *q = dm.hex_coef + 8 * (int64_t)cell + 6;
+  const float4 a = __ldg(q), b = __ldg(q + 1);   // w0..w3, w4..w7
   const float rs = r * s;
-  return fmaf(fmaf(c[7].w, t, c[4].w), rs,
-              fmaf(c[6].w, s * t, fmaf(c[5].w, r * t, fmaf(c[3].w, t, fmaf(c[2].w, s, fmaf(c[1].w, r, c[0].w))))));
+  return fmaf(fmaf(b.w, t, b.x), rs,
+              fmaf(b.z, s * t, fmaf(b.y, r * t, fmaf(a.w, t, fmaf(a.z, s, fmaf(a.y, r, a.x))))));
 }
 
 // Newton's method on x(r,s,t) - p = 0 from the guess in rst: 1 when it
@@ -85,19 +108,16 @@ __device__ __forceinline__ float hex_value(const float4 (&c)[8], float r, float 
 // (the next sample's guess along a ray). `loose` selects the kHexLooseTol
 // acceptance (the march's solves from an extrapolated guess; point location
 // from the cell centre keeps kHexNewtonTol).
-__device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const float p[3],
+__device__ __forceinline__ int hex_newton_status(const HexGeom &geo, const float p[3],
                                                  float rst[3], const float *step = nullptr,
                                                  float *drst = nullptr, bool loose = false)
 {
   float r = rst[0], s = rst[1], t = rst[2];
   bool conv = false;
+  const float (&cx)[8][3] = geo.c;
   for (int it = 0; it < kHexNewtonSteps; ++it) {
     const float rs = r * s, rt = r * t, st = s * t, rst_ = rs * t;
     float F[3], J[3][3];
-    const float cx[8][3] = {{v[0].x, v[0].y, v[0].z}, {v[1].x, v[1].y, v[1].z},
-                            {v[2].x, v[2].y, v[2].z}, {v[3].x, v[3].y, v[3].z},
-                            {v[4].x, v[4].y, v[4].z}, {v[5].x, v[5].y, v[5].z},
-                            {v[6].x, v[6].y, v[6].z}, {v[7].x, v[7].y, v[7].z}};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       F[a] = fmaf(cx[7][a], rst_, fmaf(cx[6][a], st, fmaf(cx[5][a], rt, fmaf(cx[4][a], rs,
@@ -145,9 +165,9 @@ __device__ __forceinline__ int hex_newton_status(const float4 (&v)[8], const flo
          s <= 1.f + kHexInsideTol && t >= -kHexInsideTol && t <= 1.f + kHexInsideTol;
 }
 
-__device__ __forceinline__ bool hex_newton(const float4 (&v)[8], const float p[3], float rst[3])
+__device__ __forceinline__ bool hex_newton(const HexGeom &geo, const float p[3], float rst[3])
 {
-  return hex_newton_status(v, p, rst) == 1;
+  return hex_newton_status(geo, p, rst) == 1;
 }
 
 // Face through which reference coordinates rst (outside the element) leave
@@ -170,9 +190,10 @@ __device__ __forceinline__ bool in_box(const float p[3], float lx, float ly, flo
   return !(p[0] < lx || p[1] < ly || p[2] < lz || p[0] > hx || p[1] > hy || p[2] > hz);
 }
 
-// Locate p: returns the cell id (or -1) and fills rst and the cell's corners.
+// Locate p: returns the cell id (or -1) and fills rst and the cell's
+// position coefficients.
 __device__ __forceinline__ int hex_locate(const DomainDev &dm, const float p[3], float rst[3],
-                                          float4 (&v)[8])
+                                          HexGeom &v)
 {
   if (dm.n_cells == 1) {
     hex_load(dm, 0, v);

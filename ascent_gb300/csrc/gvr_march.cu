@@ -423,7 +423,7 @@ __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, f
 __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
                          const MarchParams &mp, const float4 *lut, float thr, float4 &acc)
 {
-  float4 v[8];
+  HexGeom v;
   int cur = -1;
   float rst[3] = {0.5f, 0.5f, 0.5f};
   // change of rst from one sample to the next (J^-1 times the ray step,
@@ -487,7 +487,7 @@ __device__ int march_hex(const DomainDev &dm, const Ray &r, float t0, float t1,
     if (dm.assoc == GVR_ASSOC_ELEMENT) {
       val = __ldg(dm.cells + cur);
     } else {
-      val = hex_value(v, __saturatef(rst[0]), __saturatef(rst[1]), __saturatef(rst[2]));
+      val = hex_value(dm, cur, __saturatef(rst[0]), __saturatef(rst[1]), __saturatef(rst[2]));
     }
     const float s = __saturatef((val - mp.scalar_min) * mp.inv_range);
     const float4 col = lut_fetch(lut, mp.lut_size, mp.lut_filter, s);
@@ -1284,8 +1284,13 @@ MarchFn select(const Tuning &t, bool has_hex)
   }
   // three samples per iteration exists only at 4 CTAs per SM (at 3 it
   // measured slower than two)
-  if (t.unroll >= 3)
+  if (t.unroll >= 4)
+    return t.min_blocks >= 4 ? (t.packet_w == 4 ? pick<4, 4, 4>() : pick<8, 4, 4>())
+                             : (t.packet_w == 4 ? pick<4, 4, 3>() : pick<8, 4, 3>());
+  if (t.unroll >= 3) {
+    if (t.min_blocks < 4) return t.packet_w == 4 ? pick<4, 3, 3>() : pick<8, 3, 3>();
     return t.packet_w == 4 ? pick<4, 3, 4>() : (t.packet_w == 16 ? pick<16, 3, 4>() : pick<8, 3, 4>());
+  }
   const int u = t.unroll >= 2 ? 2 : 1;
   const int m = t.min_blocks >= 4 ? 4 : 3;
   switch (t.packet_w) {

@@ -1,9 +1,9 @@
 """Autotuner for the march kernel's launch shape.
 
 Candidates are the shapes gvr_scene_set_tuning accepts: pixel packet width
-per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1, 2,
-or 3 at 4 CTAs per SM) and the CTAs per SM the register budget targets (3
-or 4), plus the shared-memory brick staging of gvr_scene_set_staging at
+per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1 to
+4; 16-wide packets up to 3) and the CTAs per SM the register budget
+targets (3 or 4), plus the shared-memory brick staging of gvr_scene_set_staging at
 each packet width; autotune_bricks also sweeps the brick size (4^3, 8^3 or
 16^3 cells, gvr_scene_set_brick_cells), building one scene per size. Every
 candidate
@@ -25,12 +25,14 @@ from . import _native as N
 
 CANDIDATES = ([dict(packet_w=p, unroll=u, min_blocks=m)
                for p, u, m in itertools.product((8, 4, 16), (2, 1), (3, 4))] +
-              [dict(packet_w=p, unroll=3, min_blocks=4) for p in (8, 4, 16)])
+              [dict(packet_w=p, unroll=3, min_blocks=4) for p in (8, 4, 16)] +
+              [dict(packet_w=p, unroll=u, min_blocks=m)
+               for p, u, m in itertools.product((8, 4), (3, 4), (3, 4)) if (u, m) != (3, 4)])
 # shared-memory brick staging (plain path, uniform vertex scenes; elsewhere
 # the scene runs the gather kernel of the same packet shape)
 STAGED_CANDIDATES = [dict(packet_w=p, unroll=1, min_blocks=3, staged=1) for p in (8, 4, 16)]
-# the batch kernel has no 3-sample variant (it would run as 2) and no staging
-BATCH_CANDIDATES = [c for c in CANDIDATES if c["unroll"] != 3]
+# the batch kernel has no 3- or 4-sample variant (it would run as 2) and no staging
+BATCH_CANDIDATES = [c for c in CANDIDATES if c["unroll"] <= 2]
 CACHE = Path(os.environ.get("GVR_TUNE_CACHE", Path.home() / ".cache" / "gvr_tune.json"))
 
 

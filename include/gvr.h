@@ -277,8 +277,9 @@ GVR_API int gvr_scene_num_domains(const gvr_scene *scene, int *n);
 
 /* Launch shape of the scene's march kernel: pixel packet width per warp
  * (4, 8 or 16; the packet is 32 rays), samples located per loop iteration
- * (1, 2, or 3 with min_blocks 4; the batch path uses 2 for 3) and CTAs per
- * SM targeted by the register budget (3 or 4). Results do not depend on it.
+ * (1 to 4; 16-wide packets at most 3, and 3 only with min_blocks 4; the
+ * batch path uses 2 for more) and CTAs per SM targeted by the register
+ * budget (3 or 4). Results do not depend on it.
  * Set by the autotuner (ascent_gb300.tune); no counterpart in the
  * reference. */
 GVR_API int gvr_scene_set_tuning(gvr_scene *scene, int packet_w, int unroll,
