@@ -164,6 +164,8 @@ _SIGS = {
                                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                          C.POINTER(C.c_uint64)]),
     "gvr_canvas_to_rgba8": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]),
+    "gvr_canvas_color_bar": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int,
+                                       C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_void_p]),
     "gvr_composite_partials": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_int64),
                                          C.c_int, C.c_void_p]),
 }

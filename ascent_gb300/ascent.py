@@ -20,7 +20,12 @@ What each part mirrors:
   info         the `images` list of Ascent::info (rendering_filters.cpp:2024-2062)
   errors       `exceptions: forward` raises, the default prints and continues
                (ascent.cpp:218-230)
-Annotations are not drawn (the path renders the volume only).
+Annotations: the reference draws them unless a render sets
+`annotations: "false"`; this front end draws none unless a render sets
+`annotations: "true"`, and then only the body of the volume plot's colour
+bar (gvr_canvas_color_bar, at `color_bar_position` or the first default
+position, in `fg_color`): the world annotations, tick labels and field name
+are VTK-m text rendering, which is not part of this path.
 """
 from __future__ import annotations
 
@@ -364,28 +369,57 @@ class Ascent:
         render_bg = str(render.get("render_bg", "true")) != "false"
         return vr.params(w, h, bounds, data_range, single, render_bg=render_bg, bg_color=bg)
 
+    def _color_bars(self, render: dict, vr, rgba) -> None:
+        """The colour bar of the volume plot, when the render asks for
+        annotations explicitly (RenderScreenAnnotations, Render.cpp:205-227;
+        color_bar_position and fg_color parsing, rendering_filters.cpp:453-512)."""
+        if str(render.get("annotations", "false")) != "true" or \
+                str(render.get("screen_annotations", "true")) == "false":
+            return
+        box = PNG.DEFAULT_COLOR_BAR_BOXES[0]
+        if "color_bar_position" in render:
+            pos = np.asarray(render["color_bar_position"], dtype=np.float64).ravel()
+            if pos.size == 0 or pos.size % 4 != 0:
+                raise AscentError("render/color_bar_position must be an array of 4 values for each color bar")
+            box = tuple(float(x) for x in pos[:4])
+        fg = (1.0, 1.0, 1.0, 1.0)
+        if "fg_color" in render:
+            c = list(render["fg_color"])
+            if len(c) != 3:
+                raise AscentError("render/fg_color node must be an array of 3 values")
+            fg = (float(c[0]), float(c[1]), float(c[2]), 1.0)
+        tf = vr.tf
+        lut = S.color_table_sample(tf.rgb_pos, tf.rgb, tf.alpha_pos, tf.alpha, V.LUT_SIZE, N.UINT8_NONE)
+        if getattr(rgba, "dim", None) and rgba.dim() == 4:
+            for img in rgba:
+                PNG.draw_color_bar(img, lut, box, fg)
+        else:
+            PNG.draw_color_bar(rgba, lut, box, fg)
+
     def _run_render(self, sname, rname, render, sc, vr, bounds, data_range, single):
         params = self._params(vr, render, bounds, data_range, single)
         name = self._image_name(render, f"{sname}_{rname}_%04d")
         if render.get("type") == "cinema":
-            self._run_cinema(sname, rname, render, sc, params, bounds, name)
+            self._run_cinema(sname, rname, render, sc, vr, params, bounds, name)
             return
         cam = S.camera_reset_to_bounds(bounds)
         if "camera" in render:
             apply_camera(cam, render["camera"])
         rgba, depth = sc.render(cam, params, device_out=True)
+        self._color_bars(render, vr, rgba)
         path = PNG.save_canvas(self._dir / name, rgba)
         self._info["images"].append({"image_name": str(path), "image_width": params.width,
                                      "image_height": params.height, "camera": cam.as_dict(),
                                      "scene_bounds": list(map(float, bounds)), "scene": sname,
                                      "render": rname})
 
-    def _run_cinema(self, sname, rname, render, sc, params, bounds, name):
+    def _run_cinema(self, sname, rname, render, sc, vr, params, bounds, name):
         angles = cinema_angles(render)
         cams = S.cinema_cameras(bounds, angles)
         db = render.get("db_name", name)
         base = self._dir / "cinema_databases" / db / f"{self._time():g}"
         rgba, _ = sc.render_batch(cams, params, device_out=True)
+        self._color_bars(render, vr, rgba)
         lines = ["phi,theta,time,FILE"]
         for (phi, theta), img, cam in zip(angles, rgba, cams):
             fname = f"{_angle(phi)}_{_angle(theta)}_{name}.png"

@@ -18,6 +18,7 @@
 // vtkh::Image (truncation), its depth through |depth|; image i > 0 replaces
 // the kept pixel where its depth is <= 1 and not behind the kept depth; the
 // kept 8-bit colour comes back as value / 255 with its depth.
+#include <cmath>
 #include <cstdint>
 
 #include "gvr_internal.h"
@@ -37,6 +38,29 @@ rgba8_kernel(const float4 *__restrict__ rgba, int width, int height, uchar4 *__r
       return (unsigned char)__float2uint_rz(fminf(fmaxf(c * 255.f, 0.f), 255.f));
     };
     out[(int64_t)(height - 1 - y) * width + x] = make_uchar4(q(v.x), q(v.y), q(v.z), q(v.w));
+  }
+}
+
+// Colour bar body: every pixel of the bar's pixel rectangle takes the
+// colour-table entry of its position along the bar's long axis (opaque);
+// the rectangle's outermost pixels take the foreground colour.
+__global__ void __launch_bounds__(256)
+color_bar_kernel(float4 *__restrict__ rgba, int width, int x0, int y0, int bw, int bh,
+                 const float4 *__restrict__ lut, int n, int vertical, float4 fg)
+{
+  const int64_t count = (int64_t)bw * bh;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int lx = (int)(i % bw), ly = (int)(i / bw);
+    float4 c;
+    if (lx == 0 || ly == 0 || lx == bw - 1 || ly == bh - 1) {
+      c = fg;
+    } else {
+      const float t = vertical ? ((float)ly + 0.5f) / (float)bh : ((float)lx + 0.5f) / (float)bw;
+      const float4 e = lut[min((int)(t * (float)n), n - 1)];
+      c = make_float4(e.x, e.y, e.z, 1.f);
+    }
+    rgba[(int64_t)(y0 + ly) * width + (x0 + lx)] = c;
   }
 }
 
@@ -178,5 +202,57 @@ extern "C" int gvr_canvas_to_rgba8(const float *rgba, int width, int height, uin
   }
   if (scratch) cudaFreeAsync(scratch, st);
   if (e != cudaSuccess) return cuda_error(e, "canvas to rgba8");
+  return GVR_OK;
+}
+
+extern "C" int gvr_canvas_color_bar(float *rgba, int width, int height, const float *lut_rgba,
+                                    int lut_size, const float box[4], const float fg[4],
+                                    int location, void *stream)
+{
+  if (!rgba || !lut_rgba || !box || !fg) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (width < 1 || height < 1 || (int64_t)width * height > (1ll << 28))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "image size must be >= 1 and <= 2^28 pixels");
+  if (lut_size < 2 || lut_size > kMaxLut) return set_error(GVR_ERR_INVALID_ARGUMENT, "lut_size must be in [2, 4096]");
+  if (location != GVR_MEM_HOST && location != GVR_MEM_DEVICE)
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "bad location");
+  for (int k = 0; k < 4; ++k)
+    if (!std::isfinite(box[k])) return set_error(GVR_ERR_INVALID_ARGUMENT, "colour bar box must be finite");
+  if (!(box[1] > box[0]) || !(box[3] > box[2]))
+    return set_error(GVR_ERR_INVALID_ARGUMENT, "colour bar box needs xmin < xmax and ymin < ymax");
+  // screen coordinates [-1, 1] -> the pixel rectangle, clipped to the image
+  // (in double, where these products of a float and an image size are exact)
+  auto px = [](float v, int n) { return (int)std::floor(((double)v + 1.0) * 0.5 * (double)n + 0.5); };
+  const int x0 = std::max(0, px(box[0], width)), x1 = std::min(width, px(box[1], width));
+  const int y0 = std::max(0, px(box[2], height)), y1 = std::min(height, px(box[3], height));
+  if (x1 - x0 < 1 || y1 - y0 < 1) return GVR_OK;   // nothing of the bar is in the image
+  const int bw = x1 - x0, bh = y1 - y0;
+  // orientation from the requested box, as the reference's bars: taller than wide -> vertical
+  const int vertical = ((double)box[3] - box[2]) * height >= ((double)box[1] - box[0]) * width;
+  const int64_t pixels = (int64_t)width * height;
+  cudaStream_t st = (cudaStream_t)stream;
+  float4 *d_img = reinterpret_cast<float4 *>(rgba);
+  float4 *d_lut = nullptr;
+  void *scratch = nullptr;
+  const size_t lut_bytes = sizeof(float4) * lut_size;
+  cudaError_t e = scratch_alloc(&scratch, lut_bytes + (location == GVR_MEM_HOST ? sizeof(float4) * pixels : 0), st);
+  if (e != cudaSuccess) return cuda_error(e, "allocate colour bar scratch");
+  d_lut = static_cast<float4 *>(scratch);
+  e = cudaMemcpyAsync(d_lut, lut_rgba, lut_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && location == GVR_MEM_HOST) {
+    d_img = d_lut + lut_size;
+    e = cudaMemcpyAsync(d_img, rgba, sizeof(float4) * pixels, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) {
+    const int grid = (int)std::min<int64_t>(((int64_t)bw * bh + 255) / 256, 152 * 8);
+    color_bar_kernel<<<grid, 256, 0, st>>>(d_img, width, x0, y0, bw, bh, d_lut, lut_size, vertical,
+                                           make_float4(fg[0], fg[1], fg[2], fg[3]));
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && location == GVR_MEM_HOST)
+    e = cudaMemcpyAsync(rgba, d_img, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the LUT was copied from host memory
+  cudaFreeAsync(scratch, st);
+  if (e != cudaSuccess) return cuda_error(e, "colour bar");
   return GVR_OK;
 }

@@ -48,6 +48,41 @@ def canvas_to_rgba8_device(rgba):
     return out
 
 
+# default colour bar positions of the reference's Annotator (Annotator.cpp:15-24):
+# {xmin, xmax, ymin, ymax} in screen coordinates, one per plot with a table
+DEFAULT_COLOR_BAR_BOXES = ((0.84, 0.92, 0.1, 0.8), (0.84, 0.92, -0.8, -0.1),
+                           (-0.8, -0.72, 0.1, 0.8), (-0.8, -0.72, -0.8, -0.1))
+
+
+def draw_color_bar(canvas, lut, box=DEFAULT_COLOR_BAR_BOXES[0], fg=(1.0, 1.0, 1.0, 1.0)):
+    """Draw a colour bar's body into a float canvas in place
+    (gvr_canvas_color_bar): a (H, W, 4) float32 numpy array or CUDA tensor,
+    the colour table as (n, 4) RGBA rows, box = (xmin, xmax, ymin, ymax) in
+    screen coordinates. Labels and ticks are not drawn."""
+    import ctypes as C
+
+    from . import _native as N
+    lut = np.ascontiguousarray(lut, dtype=np.float32).reshape(-1, 4)
+    b = (C.c_float * 4)(*[float(x) for x in box])
+    f = (C.c_float * 4)(*[float(x) for x in fg])
+    if isinstance(canvas, np.ndarray):
+        if canvas.dtype != np.float32 or canvas.ndim != 3 or canvas.shape[2] != 4 or not canvas.flags.c_contiguous:
+            raise ValueError("canvas must be a C-contiguous (H, W, 4) float32 array")
+        h, w, _ = canvas.shape
+        N.call("gvr_canvas_color_bar", C.c_void_p(canvas.ctypes.data), w, h, N.fptr(lut), lut.shape[0], b, f,
+               N.MEM_HOST, None)
+        return canvas
+    import torch
+    if canvas.dtype != torch.float32 or not canvas.is_cuda or canvas.dim() != 3 or canvas.shape[2] != 4 \
+            or not canvas.is_contiguous():
+        raise ValueError("canvas must be a contiguous (H, W, 4) float32 CUDA tensor")
+    h, w, _ = canvas.shape
+    stream = torch.cuda.current_stream(canvas.device).cuda_stream
+    N.call("gvr_canvas_color_bar", C.c_void_p(canvas.data_ptr()), w, h, N.fptr(lut), lut.shape[0], b, f,
+           N.MEM_DEVICE, C.c_void_p(stream))
+    return canvas
+
+
 def _chunk(tag: bytes, data: bytes) -> bytes:
     return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
 

@@ -462,6 +462,22 @@ GVR_API int gvr_composite_partials(const gvr_partial *partials, int64_t n, gvr_p
 GVR_API int gvr_canvas_to_rgba8(const float *rgba, int width, int height, uint8_t *out,
                                 int location, void *stream);
 
+/* Draw the body of a colour bar into a float canvas (width x height, RGBA,
+ * row 0 at the bottom): the pixels of `box` = {xmin, xmax, ymin, ymax} in
+ * screen coordinates [-1, 1] (clipped to the image) take the colour-table
+ * entry of their position along the box's long axis (vertical when the box
+ * is taller than wide, low values at the bottom / left), opaque; the
+ * rectangle's outermost pixels take `fg`. This is the coloured part of the
+ * bars Render::RenderScreenAnnotations draws for each plot's colour table
+ * (vtkh/rendering/Render.cpp:205-227, positions of Annotator.cpp:15-24, or
+ * the render's `color_bar_position`); the tick marks, labels and field name
+ * the reference draws with VTK-m's text rendering are not drawn. lut_rgba
+ * is a host array of lut_size RGBA entries (2 .. 4096); the canvas lives
+ * where `location` says. Returns when the bar is drawn. */
+GVR_API int gvr_canvas_color_bar(float *rgba, int width, int height, const float *lut_rgba,
+                                 int lut_size, const float box[4], const float fg[4],
+                                 int location, void *stream);
+
 /* gvr_composite_partials for device records whose pixel ids the caller
  * bounds, without any host synchronisation; no counterpart in the
  * reference (its composite is host code). Every record's pixel_id must lie

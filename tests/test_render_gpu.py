@@ -379,3 +379,46 @@ def test_named_preset_against_oracle(name):
     wl.rgb_pos, wl.rgb, wl.alpha_pos, wl.alpha = ctw.rgb_pos, ctw.rgb, ctw.alpha_pos, ctw.alpha
     (g2, _, _), _, _ = render_both(wl)
     assert np.abs(g2 - g).max() > 0.05
+
+
+def test_sixty_four_domains_and_the_limit():
+    """The most domains one render composites (64: a 4 x 4 x 4 split), against
+    the oracle; a 65th domain is refused with a clear error."""
+    wl = W.plain_small(n=41, width=96, height=80, parts=(4, 4, 4))
+    assert len(wl.domains) == 64
+    (g, gd, gn), (o, od, on), _ = render_both(wl)
+    assert_parity(g, o)
+    assert abs(gn - on) <= 1e-3 * on
+    assert_depth(gd, od)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        d = wl.domains[0]
+        with pytest.raises(N.GvrError) as err:
+            sc.add_uniform(d.field, d.origin, d.spacing)
+        assert err.value.code == N.GVR_ERR_UNSUPPORTED
+
+
+def test_two_node_domains():
+    """Domains of a single cell (2 nodes per axis) side by side: the smallest
+    bricks (one cell, padded) render like the oracle."""
+    rng = np.random.default_rng(9)
+    with S.Scene(0) as sc:
+        osc = O.OracleScene(64)
+        for i in range(3):
+            for j in range(2):
+                f = rng.uniform(0, 1, (2, 2, 2)).astype(np.float32)
+                origin = (0.5 * i, 0.5 * j, 0.0)
+                sc.add_uniform(f, origin, (0.5, 0.5, 0.5))
+                osc.add_uniform((2, 2, 2), origin, (0.5, 0.5, 0.5), f)
+        bounds = sc.bounds()
+        cam = S.camera_reset_to_bounds(bounds)
+        S.camera_azimuth(cam, 20.0)
+        S.camera_elevation(cam, 25.0)
+        x = np.linspace(0, 1, 64)
+        lut = np.stack([x, 1 - x, 0.5 * np.ones_like(x), 0.05 * x], 1).astype(np.float32)
+        p = N.make_params(64, 48, S.sample_distance(bounds, 200), (0.0, 1.0), lut)
+        g, _, gn = sc.render(cam, p, count_samples=True)
+    o, _, on = osc.render(cam, p)
+    assert o[..., 3].max() > 0.05
+    assert_parity(g, o)
+    assert abs(gn - on) <= 1e-3 * on + 2
