@@ -39,7 +39,8 @@ CACHE = Path(os.environ.get("GVR_TUNE_CACHE", Path.home() / ".cache" / "gvr_tune
 def _key(scene, params) -> str:
     import torch
     name = torch.cuda.get_device_name(scene.device).replace(" ", "_")
-    return f"{name}|dom{scene.num_domains}|{params.width}x{params.height}|lut{params.lut_size}"
+    cells = getattr(scene, "brick_cells", 8)
+    return f"{name}|dom{scene.num_domains}|{params.width}x{params.height}|lut{params.lut_size}|brick{cells}"
 
 
 def _time(scene, camera, params, rgba, depth, stream, reps: int) -> float:
