@@ -107,6 +107,7 @@ _SIGS = {
     "gvr_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
     "gvr_scratch_trim": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(C.c_uint64)]),
     "gvr_scene_set_staging": (C.c_int, [C.c_void_p, C.c_int]),
+    "gvr_scene_set_tile_order": (C.c_int, [C.c_void_p, C.c_int]),
     "gvr_scene_set_brick_cells": (C.c_int, [C.c_void_p, C.c_int]),
     "gvr_scene_staging_failures": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "gvr_composite_partials_async": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,

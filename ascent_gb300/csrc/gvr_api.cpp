@@ -459,6 +459,7 @@ int gvr_scene_destroy(gvr_scene *s)
   cudaFree(s->d_rects);
   cudaFree(s->d_queue);
   for (auto &t : s->tile_orders) cudaFree(t.second);
+  cudaFree(s->d_cost_order);
   cudaFree(s->d_batch_rgba);
   cudaFree(s->d_batch_depth);
   if (s->batch_exec) cudaGraphExecDestroy(s->batch_exec);
@@ -1141,6 +1142,14 @@ int gvr_scene_set_staging(gvr_scene *s, int mode)
   return GVR_OK;
 }
 
+int gvr_scene_set_tile_order(gvr_scene *s, int mode)
+{
+  if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (mode != 0 && mode != 1) return set_error(GVR_ERR_INVALID_ARGUMENT, "tile order mode must be 0 or 1");
+  s->tuning.tile_order = mode;
+  return GVR_OK;
+}
+
 int gvr_scene_staging_failures(const gvr_scene *s, uint64_t *n)
 {
   if (!s || !n) return set_error(GVR_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -1209,7 +1218,23 @@ static int render_one(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
     mp.canvas_depth = d_depth;
   }
   const int *d_order = nullptr;
-  if ((rc = tile_order(s, p->width, p->height, &d_order)) != GVR_OK) return rc;
+  const int64_t n_tiles = (int64_t)((p->width + kMarchTile - 1) / kMarchTile) *
+                          ((p->height + kMarchTile - 1) / kMarchTile);
+  if (s->tuning.tile_order == 1 && n_tiles <= kCostOrderTiles) {
+    if (s->cost_order_cap < n_tiles) {
+      cudaFree(s->d_cost_order);
+      s->d_cost_order = nullptr;
+      s->cost_order_cap = 0;
+      e = cudaMalloc(&s->d_cost_order, sizeof(int) * n_tiles);
+      if (e != cudaSuccess) return cuda_error(e, "cudaMalloc tile cost order");
+      s->cost_order_cap = n_tiles;
+    }
+    e = launch_tile_cost_order(s->d_domains, view, mp, s->d_cost_order, st);
+    if (e != cudaSuccess) return cuda_error(e, "tile cost order launch");
+    d_order = s->d_cost_order;
+  } else if ((rc = tile_order(s, p->width, p->height, &d_order)) != GVR_OK) {
+    return rc;
+  }
   StageOrder order;
   if (s->tuning.staged && staged_order(s, camera->position, order)) {
     e = launch_staged(s->d_domains, view, mp, s->d_lut, d_rgba, d_depth,

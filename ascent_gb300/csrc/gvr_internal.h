@@ -75,6 +75,8 @@ struct Tuning {
   int min_blocks = 4;
   int tiles_per_item = 1;   // batch path: 16x16 tiles per work-queue item
   int staged = 0;           // plain path: stage bricks in shared memory (uniform vertex scenes)
+  int tile_order = 0;       // plain path: 0 = tiles nearest the image centre first,
+                            // 1 = longest-first by the view's estimated tile cost
 };
 
 // Front-to-back order of a scene's domains for one view (staged march).
@@ -214,6 +216,10 @@ struct gvr_scene {
   // launch order of the march kernel's tiles per tile grid (linear tile
   // indices, nearest the image centre first); written once, then read only
   std::map<std::pair<int, int>, int *> tile_orders;
+  // per-view longest-first tile order (tile_order 1), rewritten by every
+  // render that uses it
+  int *d_cost_order = nullptr;
+  int64_t cost_order_cap = 0;
 };
 
 namespace gvr {
@@ -291,6 +297,12 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          float4 *d_rgba, float *d_depth,
                          unsigned long long *d_samples, const Tuning &tuning,
                          bool has_hex, const int *d_order, cudaStream_t stream);
+// longest-first tile order for one view (gvr_march.cu): writes a permutation
+// of the view's kMarchTile tiles to d_order (one int per tile); grids of more
+// than kCostOrderTiles tiles are refused (cudaErrorInvalidValue)
+constexpr int kCostOrderTiles = 48 * 1024;
+cudaError_t launch_tile_cost_order(const DomainDev *d_domains, const ViewDev &view, const MarchParams &mp,
+                                   int *d_order, cudaStream_t stream);
 // staged march (gvr_march.cu): uniform vertex-field domains only, taken in
 // `order`; *d_stage_fail counts CTAs whose bounded wait for their bulk
 // copies gave up (they finish from global memory)

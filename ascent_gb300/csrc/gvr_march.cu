@@ -1323,6 +1323,92 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
 }
 
 
+// Longest-first launch order of the march tiles for one view: the cost of a
+// tile is the summed length, through every domain box, of five of its rays
+// (its centre and corner pixels); tiles are counting-sorted into 1024 cost
+// bins, longest first, so that the last tiles the GPU takes are the short
+// ones (longest-processing-time-first list scheduling). One CTA; the order
+// of tiles within a bin is whatever the shared-memory atomics give, and no
+// order changes a pixel. Dynamic shared memory: one int per tile.
+__global__ void __launch_bounds__(1024)
+tile_cost_order_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ ViewDev view,
+                       const __grid_constant__ MarchParams mp, int *__restrict__ order)
+{
+  extern __shared__ int s_key[];
+  __shared__ int s_hist[1024];
+  __shared__ int s_warp[32];
+  __shared__ unsigned s_max;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tiles_x = (mp.width + kTile - 1) / kTile;
+  const int n = tiles_x * ((mp.height + kTile - 1) / kTile);
+  s_hist[tid] = 0;
+  if (tid == 0) s_max = 0u;
+  __syncthreads();
+  for (int t = tid; t < n; t += 1024) {
+    const int x0 = (t % tiles_x) * kTile, y0 = (t / tiles_x) * kTile;
+    const int x1 = min(x0 + kTile - 1, mp.width - 1), y1 = min(y0 + kTile - 1, mp.height - 1);
+    const int rx[5] = {(x0 + x1) >> 1, x0, x1, x0, x1};
+    const int ry[5] = {(y0 + y1) >> 1, y0, y0, y1, y1};
+    float cost = 0.f;
+    for (int k = 0; k < 5; ++k) {
+      const Ray r = pixel_ray(view, mp, rx[k], ry[k]);
+      for (int d = 0; d < mp.n_domains; ++d) {
+        float t0, t1;
+        if (slab(g_domains[d], r, t0, t1)) cost += t1 - t0;
+      }
+    }
+    cost = cost > 0.f && cost < FLT_MAX ? cost : 0.f;   // NaN and inf cost nothing
+    s_key[t] = __float_as_int(cost);
+    atomicMax(&s_max, __float_as_uint(cost));
+  }
+  __syncthreads();
+  const float top = __uint_as_float(s_max);
+  const float scale = top > 0.f ? 1023.f / top : 0.f;
+  for (int t = tid; t < n; t += 1024) {
+    const int k = 1023 - min(1023, (int)(__int_as_float(s_key[t]) * scale));
+    s_key[t] = k;
+    atomicAdd(&s_hist[k], 1);
+  }
+  __syncthreads();
+  // exclusive scan of the 1024 bins, one per thread
+  const int v = s_hist[tid];
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = s_warp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    s_warp[lane] = w;
+  }
+  __syncthreads();
+  s_hist[tid] = x - v + (warp ? s_warp[warp - 1] : 0);
+  __syncthreads();
+  for (int t = tid; t < n; t += 1024) order[atomicAdd(&s_hist[s_key[t]], 1)] = t;
+}
+
+cudaError_t launch_tile_cost_order(const DomainDev *d_domains, const ViewDev &view, const MarchParams &mp,
+                                   int *d_order, cudaStream_t stream)
+{
+  const int64_t tiles = (int64_t)((mp.width + kTile - 1) / kTile) * ((mp.height + kTile - 1) / kTile);
+  if (tiles > kCostOrderTiles) return cudaErrorInvalidValue;
+  const size_t smem = sizeof(int) * (size_t)tiles;
+  cudaError_t e = cudaFuncSetAttribute(tile_cost_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(int) * kCostOrderTiles));
+  if (e != cudaSuccess) return e;
+  tile_cost_order_kernel<<<1, 1024, smem, stream>>>(d_domains, view, mp, d_order);
+  count_launch();
+  return cudaGetLastError();
+}
+
 namespace {
 
 using StagedFn = void (*)(const DomainDev *, const ViewDev, const MarchParams, const float4 *, float4 *,

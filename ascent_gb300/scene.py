@@ -164,12 +164,15 @@ class Scene:
         N.call("gvr_scene_update_fields", self.handle, len(args), ids, ptrs, code, 1, loc, st)
         del args
 
-    def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4, staged: int = 0) -> None:
-        """Launch shape of the march kernel and whether the plain path stages
-        bricks in shared memory; images do not depend on either."""
+    def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4, staged: int = 0,
+                   tile_order: int = 0) -> None:
+        """Launch shape of the march kernel, whether the plain path stages
+        bricks in shared memory and how it orders its tiles (0 centre
+        first, 1 longest first for each view); images depend on none."""
         N.call("gvr_scene_set_tuning", self.handle, int(packet_w), int(unroll), int(min_blocks))
         N.call("gvr_scene_set_staging", self.handle, int(staged))
-        self.tuning = (int(packet_w), int(unroll), int(min_blocks), int(staged))
+        N.call("gvr_scene_set_tile_order", self.handle, int(tile_order))
+        self.tuning = (int(packet_w), int(unroll), int(min_blocks), int(staged), int(tile_order))
 
     def staging_failures(self) -> int:
         """Tiles whose bounded wait for staged bricks gave up (0 normally)."""

@@ -4,7 +4,8 @@ Candidates are the shapes gvr_scene_set_tuning accepts: pixel packet width
 per warp (4x8, 8x4, 16x2 rays), samples located per loop iteration (1 to
 4; 16-wide packets up to 3) and the CTAs per SM the register budget
 targets (3 or 4), plus the shared-memory brick staging of gvr_scene_set_staging at
-each packet width; autotune_bricks also sweeps the brick size (4^3, 8^3 or
+each packet width; the winner is then timed with each tile launch order of
+gvr_scene_set_tile_order (centre first, or longest first per view); autotune_bricks also sweeps the brick size (4^3, 8^3 or
 16^3 cells, gvr_scene_set_brick_cells), building one scene per size. Every
 candidate
 renders the caller's own view on the caller's scene; the fastest median of
@@ -125,6 +126,12 @@ def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True, stage
         name = f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}" + ("s" if cand.get("staged") else "")
         results[name] = (_time(scene, camera, params, rgba, depth, stream, reps), cand)
     name, (ms, best) = min(results.items(), key=lambda kv: kv[1][0])
+    # the winner again with each tile order, timed back to back
+    for order in (0, 1):
+        cand = dict(best, tile_order=order)
+        scene.set_tuning(**cand)
+        results[name + f"o{order}"] = (_time(scene, camera, params, rgba, depth, stream, 2 * reps), cand)
+    best = min((results[name + "o0"], results[name + "o1"]), key=lambda r: r[0])[1]
     scene.set_tuning(**best)
     out = {"best": best, "ms": {k: round(v[0], 4) for k, v in results.items()}, "cached": False}
     if use_cache:

@@ -71,6 +71,12 @@ def parse_args():
     return ap.parse_args()
 
 
+def tile_order_ms(tuning: dict) -> dict:
+    """The tuner's back-to-back timings of its winning shape with the
+    centre-first (o0) and longest-first (o1) tile orders."""
+    return {k: v for k, v in tuning.get("ms", {}).items() if k.endswith(("o0", "o1"))}
+
+
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -328,7 +334,7 @@ def bench_hex(dev, n_cells=200, size=1024, reps=5):
             "cpu_port_gsamples_per_s": cpu["value"], "cpu_cores": cpu["cores"],
             "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
             "bvh_build_ms": build_ms, "face_neighbour_build_ms": nbr_ms, "load_s": round(load_s, 2), "generate_s": round(gen_s, 2),
-            "tuning": tuning["best"],
+            "tuning": tuning["best"], "tile_order_ms": tile_order_ms(tuning),
             "roofline": {"bound": "hbm", "achieved": alg / ms / 1e6, "peak": pk["hbm_gbs"],
                          "unit": "GB/s", "frac": alg / ms / 1e6 / pk["hbm_gbs"],
                          "bytes_per_sample": 160}}
@@ -636,6 +642,7 @@ def bench_plain_small(dev, reps=20) -> dict:
     ocam, op = oracle_setup(wl)
     return {"workload": wl.name, "samples_per_frame": n, "gsamples_per_s": n / ms / 1e6,
             "fps": 1e3 / ms, "ms_per_frame": ms, "tuning": tuning["best"],
+            "tile_order_ms": tile_order_ms(tuning),
             "cpu_port_gsamples_per_s": cpu["value"],
             "speedup_vs_cpu_port": n / ms / 1e6 / cpu["value"],
             "error_vs_fp64_oracle": accuracy(dev, wl, [cam], p, [ocam], op)}
