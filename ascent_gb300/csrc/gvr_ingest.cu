@@ -130,7 +130,7 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
                                           int *__restrict__ timed_out, long long first_polls)
 {
   __shared__ __align__(16) float rows[kRows * kRowSlot];
-  __shared__ int lead[kRows];
+  __shared__ int rowbase[kRows + 1];   // first node of row r in `rows`; one spare entry
   __shared__ int plain[kRows];
   __shared__ __align__(8) uint64_t bar;
   const int x0 = run * kRunBricks * kBrickCells;
@@ -154,12 +154,15 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
   // thread r plans row r: announces its bytes on the barrier and issues its
   // bulk copy (or marks the row for plain loads); thread 0 arrives once all
   // rows are announced, so the phase cannot complete early
+  int my_plain = 0;
+  if (threadIdx.x == kRows) rowbase[kRows] = 0;
   if (threadIdx.x < kRows) {
     const int r = threadIdx.x;
     uintptr_t a;
     unsigned sz;
-    lead[r] = row_range(r, a, sz);
-    plain[r] = (a < base || a + sz > end) ? 1 : 0;
+    rowbase[r] = r * kRowSlot + row_range(r, a, sz);
+    my_plain = (a < base || a + sz > end) ? 1 : 0;
+    plain[r] = my_plain;
     if (!plain[r]) {
       asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)),
                    "r"(sz)
@@ -171,18 +174,21 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
           : "memory");
     }
   }
-  __syncthreads();
+  const bool any_plain = __syncthreads_or(my_plain);
   if (threadIdx.x == 0)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
   __syncthreads();
   bool ok = mbar_wait_bounded(&bar, first_polls);
-  // rows that could not be copied in bulk: plain loads
-  for (int r = 0; r < kRows; ++r) {
-    if (!plain[r]) continue;
-    const int y = min(by * kBrickCells + r % kBrickNodes, ny - 1);
-    const int z = min(bz * kBrickCells + r / kBrickNodes, nz - 1);
-    const float *row = src + ((int64_t)z * ny + y) * nx + x0;
-    for (int i = threadIdx.x; i < count; i += blockDim.x) rows[r * kRowSlot + lead[r] + i] = row[i];
+  // rows that could not be copied in bulk (only next to the end of the
+  // field's buffer): plain loads
+  if (any_plain) {
+    for (int r = 0; r < kRows; ++r) {
+      if (!plain[r]) continue;
+      const int y = min(by * kBrickCells + r % kBrickNodes, ny - 1);
+      const int z = min(bz * kBrickCells + r / kBrickNodes, nz - 1);
+      const float *row = src + ((int64_t)z * ny + y) * nx + x0;
+      for (int i = threadIdx.x; i < count; i += blockDim.x) rows[rowbase[r] + i] = row[i];
+    }
   }
   if (!ok) {
     atomicOr(timed_out, 1);
@@ -195,26 +201,41 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
     mbar_wait_bounded(&bar, kStageSpin);
   }
   __syncthreads();
-  // warp w writes bricks run * 16 + w and run * 16 + 8 + w
+  // warp w writes bricks run * 16 + w and run * 16 + 8 + w, four nodes per
+  // lane and step (one 16-byte store; a brick is 184 float4). Four
+  // consecutive nodes cross at most one node row (rows hold 9), so each
+  // step reads two row bases and no division per node.
+  static_assert(kBrickFloats % 4 == 0 && kBrickNodes > 4, "float4 steps over 9-node rows");
+  constexpr int kNodes = kBrickNodes * kBrickNodes * kBrickNodes;   // 729
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int x_last = nx - 1 - x0;   // last node of the field, relative to the run
   for (int half = 0; half < kRunBricks / 8; ++half) {
     const int bx = run * kRunBricks + half * 8 + w;
     if (bx >= nbx) return;
     const int64_t b = ((int64_t)bz * nby + by) * nbx + bx;
-    float *dst = bricks + b * kBrickFloats;
+    float4 *dst = reinterpret_cast<float4 *>(bricks + b * kBrickFloats);
+    const int xb = bx * kBrickCells - x0;
     float vmin = FLT_MAX, vmax = -FLT_MAX;
     int bad = !ok;
-    for (int l = lane; l < kBrickFloats; l += 32) {
-      float v = 0.f;
-      if (l < kBrickNodes * kBrickNodes * kBrickNodes) {
-        const int lx = l % kBrickNodes, rr = l / kBrickNodes;
-        const int x = min(bx * kBrickCells + lx, nx - 1) - x0;
-        v = rows[rr * kRowSlot + lead[rr] + x];
-        bad |= !isfinite(v);
-        vmin = fminf(vmin, v);
-        vmax = fmaxf(vmax, v);
+    for (int q = lane; q < kBrickFloats / 4; q += 32) {
+      const int l = 4 * q;
+      const int rr = l / kBrickNodes, lx = l - kBrickNodes * rr;
+      const int rb0 = rowbase[rr], rb1 = rowbase[rr + 1];
+      float v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const bool same = lx + k < kBrickNodes;
+        const int node = same ? lx + k : lx + k - kBrickNodes;
+        float t = 0.f;
+        if (l + k < kNodes) {
+          t = rows[(same ? rb0 : rb1) + min(xb + node, x_last)];
+          bad |= !isfinite(t);
+          vmin = fminf(vmin, t);
+          vmax = fmaxf(vmax, t);
+        }
+        v[k] = t;
       }
-      dst[l] = v;
+      dst[q] = make_float4(v[0], v[1], v[2], v[3]);
     }
     bad = __any_sync(0xffffffffu, bad);
     for (int o = 16; o > 0; o >>= 1) {
@@ -225,7 +246,7 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
   }
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)   // 5 CTAs per SM: 44 KB of rows each
 brick_staged_kernel(const float *__restrict__ src, int64_t n_src, int nx, int ny, int nz, int nbx,
                     int nby, float *__restrict__ bricks, float2 *__restrict__ brick_range,
                     int *__restrict__ timed_out, long long first_polls)
@@ -250,7 +271,7 @@ struct StagedJobs {
   int n;
 };
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)   // 5 CTAs per SM: 44 KB of rows each
 brick_staged_multi_kernel(const __grid_constant__ StagedJobs jobs, int *__restrict__ timed_out,
                           long long first_polls)
 {
