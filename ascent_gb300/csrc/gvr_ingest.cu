@@ -130,9 +130,11 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
                                           int *__restrict__ timed_out, long long first_polls)
 {
   __shared__ __align__(16) float rows[kRows * kRowSlot];
-  __shared__ int rowbase[kRows + 1];   // first node of row r in `rows`; one spare entry
-  __shared__ int plain[kRows];
+  // brick node l's place in `rows`, less the brick's first x: its row's slot
+  // plus the row copy's lead plus its x within the brick (< 2^16)
+  __shared__ unsigned short nodeoff[kBrickNodes * kBrickNodes * kBrickNodes];
   __shared__ __align__(8) uint64_t bar;
+  static_assert(kRows * kRowSlot < 65536, "node offsets fit 16 bits");
   const int x0 = run * kRunBricks * kBrickCells;
   const int count = min(kRunNodes, nx - x0);
   const uintptr_t base = reinterpret_cast<uintptr_t>(src);
@@ -155,15 +157,13 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
   // bulk copy (or marks the row for plain loads); thread 0 arrives once all
   // rows are announced, so the phase cannot complete early
   int my_plain = 0;
-  if (threadIdx.x == kRows) rowbase[kRows] = 0;
   if (threadIdx.x < kRows) {
     const int r = threadIdx.x;
     uintptr_t a;
     unsigned sz;
-    rowbase[r] = r * kRowSlot + row_range(r, a, sz);
+    row_range(r, a, sz);
     my_plain = (a < base || a + sz > end) ? 1 : 0;
-    plain[r] = my_plain;
-    if (!plain[r]) {
+    if (!my_plain) {
       asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)),
                    "r"(sz)
                    : "memory");
@@ -177,17 +177,28 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
   const bool any_plain = __syncthreads_or(my_plain);
   if (threadIdx.x == 0)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  // while the copies are in flight: every brick node's offset in `rows`
+  constexpr int kNodes = kBrickNodes * kBrickNodes * kBrickNodes;   // 729
+  for (int l = threadIdx.x; l < kNodes; l += blockDim.x) {
+    const int rr = l / kBrickNodes;
+    uintptr_t a;
+    unsigned sz;
+    nodeoff[l] = (unsigned short)(rr * kRowSlot + row_range(rr, a, sz) + (l - kBrickNodes * rr));
+  }
   __syncthreads();
   bool ok = mbar_wait_bounded(&bar, first_polls);
   // rows that could not be copied in bulk (only next to the end of the
   // field's buffer): plain loads
   if (any_plain) {
     for (int r = 0; r < kRows; ++r) {
-      if (!plain[r]) continue;
+      uintptr_t a;
+      unsigned sz;
+      const int lead = row_range(r, a, sz);
+      if (!(a < base || a + sz > end)) continue;
       const int y = min(by * kBrickCells + r % kBrickNodes, ny - 1);
       const int z = min(bz * kBrickCells + r / kBrickNodes, nz - 1);
       const float *row = src + ((int64_t)z * ny + y) * nx + x0;
-      for (int i = threadIdx.x; i < count; i += blockDim.x) rows[rowbase[r] + i] = row[i];
+      for (int i = threadIdx.x; i < count; i += blockDim.x) rows[r * kRowSlot + lead + i] = row[i];
     }
   }
   if (!ok) {
@@ -201,42 +212,49 @@ __device__ __forceinline__ void brick_run(const float *__restrict__ src, int64_t
     mbar_wait_bounded(&bar, kStageSpin);
   }
   __syncthreads();
-  // warp w writes bricks run * 16 + w and run * 16 + 8 + w, four nodes per
-  // lane and step (one 16-byte store; a brick is 184 float4). Four
-  // consecutive nodes cross at most one node row (rows hold 9), so each
-  // step reads two row bases and no division per node.
-  static_assert(kBrickFloats % 4 == 0 && kBrickNodes > 4, "float4 steps over 9-node rows");
-  constexpr int kNodes = kBrickNodes * kBrickNodes * kBrickNodes;   // 729
+  // warp w writes bricks run * 16 + w and run * 16 + 8 + w: lane i takes
+  // nodes i, i + 32, ... (consecutive lanes read neighbouring nodes of a
+  // row, so the shared-memory reads hardly conflict, and store 128
+  // contiguous bytes per warp and step). A brick whose nodes all lie in the
+  // field reads them at nodeoff + its first x; the last brick of a row that
+  // ends inside a brick clamps x to the field's last node.
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int x_last = nx - 1 - x0;   // last node of the field, relative to the run
   for (int half = 0; half < kRunBricks / 8; ++half) {
     const int bx = run * kRunBricks + half * 8 + w;
     if (bx >= nbx) return;
     const int64_t b = ((int64_t)bz * nby + by) * nbx + bx;
-    float4 *dst = reinterpret_cast<float4 *>(bricks + b * kBrickFloats);
+    float *dst = bricks + b * kBrickFloats;
     const int xb = bx * kBrickCells - x0;
     float vmin = FLT_MAX, vmax = -FLT_MAX;
-    int bad = !ok;
-    for (int q = lane; q < kBrickFloats / 4; q += 32) {
-      const int l = 4 * q;
-      const int rr = l / kBrickNodes, lx = l - kBrickNodes * rr;
-      const int rb0 = rowbase[rr], rb1 = rowbase[rr + 1];
-      float v[4];
+    float nf = 0.f;   // 0 * node summed: NaN once a node is NaN or infinite
+    if (xb + kBrickCells <= x_last) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const bool same = lx + k < kBrickNodes;
-        const int node = same ? lx + k : lx + k - kBrickNodes;
+      for (int s = 0; s < kBrickFloats / 32; ++s) {
+        const int l = lane + 32 * s;
         float t = 0.f;
-        if (l + k < kNodes) {
-          t = rows[(same ? rb0 : rb1) + min(xb + node, x_last)];
-          bad |= !isfinite(t);
+        if (l < kNodes) {
+          t = rows[nodeoff[l] + xb];
+          nf = fmaf(t, 0.f, nf);
           vmin = fminf(vmin, t);
           vmax = fmaxf(vmax, t);
         }
-        v[k] = t;
+        dst[l] = t;
       }
-      dst[q] = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+      for (int l = lane; l < kBrickFloats; l += 32) {
+        float t = 0.f;
+        if (l < kNodes) {
+          const int node = l % kBrickNodes;
+          t = rows[nodeoff[l] - node + min(xb + node, x_last)];
+          nf = fmaf(t, 0.f, nf);
+          vmin = fminf(vmin, t);
+          vmax = fmaxf(vmax, t);
+        }
+        dst[l] = t;
+      }
     }
+    int bad = !ok || !(nf == 0.f);
     bad = __any_sync(0xffffffffu, bad);
     for (int o = 16; o > 0; o >>= 1) {
       vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
