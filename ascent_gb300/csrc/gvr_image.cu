@@ -85,15 +85,20 @@ zbuffer_kernel(const ZImages images, int n_images, int64_t n, float4 *__restrict
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    // Image::Init of the first image: 8-bit colour, |depth|
-    uchar4 c = to_u8(images.rgba[0][i]);
+    // Image::Init of the first image: 8-bit colour, |depth|; each later
+    // image that passes ZBufferComposite's test replaces both, so the
+    // result is the last winner's colour: the depths are tested first (all
+    // loads independent) and only the winner's colour is read
     float d = fabsf(images.depth[0][i]);
+    int win = 0;
+#pragma unroll 8
     for (int k = 1; k < n_images; ++k) {
       const float dk = fabsf(images.depth[k][i]);
       if (dk > 1.f || d < dk) continue;   // ZBufferComposite's test
       d = dk;
-      c = to_u8(images.rgba[k][i]);
+      win = k;
     }
+    const uchar4 c = to_u8(images.rgba[win][i]);
     const float s = 1.f / 255.f;          // ImageToCanvas
     out_rgba[i] = make_float4((float)c.x * s, (float)c.y * s, (float)c.z * s, (float)c.w * s);
     out_depth[i] = d;
