@@ -1087,7 +1087,7 @@ static bool staged_order(const gvr_scene *s, const float eye[3], StageOrder &out
   for (int i = 0; i < n; ++i) {
     for (int j = i + 1; j < n; ++j) {
       const double *bi = s->domains[i].bounds, *bj = s->domains[j].bounds;
-      int verdict = 0;      // +1: i first, -1: j first
+      int vote = 0;          // +1: i first, -1: j first
       bool conflict = false;
       for (int a = 0; a < 3; ++a) {
         int v = 0;
@@ -1099,12 +1099,12 @@ static bool staged_order(const gvr_scene *s, const float eye[3], StageOrder &out
           else if (eye[a] > bi[2 * a]) v = 1;
         }
         if (v != 0) {
-          if (verdict != 0 && verdict != v) conflict = true;
-          verdict = v;
+          if (vote != 0 && vote != v) conflict = true;
+          vote = v;
         }
       }
-      if (conflict || verdict == 0) continue;
-      if (verdict > 0) before[j] |= 1ull << i;
+      if (conflict || vote == 0) continue;
+      if (vote > 0) before[j] |= 1ull << i;
       else before[i] |= 1ull << j;
     }
   }

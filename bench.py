@@ -545,6 +545,14 @@ def bench_composite(dev, n_images=8, size=1024, cover=0.8, reps=10) -> dict:
     async_ms = _timed(lambda: CP.composite_partials_device_async(d, 0, size * size - 1, out=aout, n_out=an),
                       stream, reps)
     async_exact = CP.from_device(aout[: int(an.item())]).tobytes() == ref.tobytes()
+    # the same call through the C ABI with its arguments built once
+    import ctypes as C
+    from ascent_gb300 import _native as N
+    cargs = (d.data_ptr(), d.shape[0], 0, size * size - 1, aout.data_ptr(), an.data_ptr(),
+             C.c_void_p(stream.cuda_stream))
+    for _ in range(3):
+        N.call("gvr_composite_partials_async", *cargs)
+    cabi_ms = _timed(lambda: N.call("gvr_composite_partials_async", *cargs), stream, reps)
     t0 = time.perf_counter()
     O.composite_partials(ims, precision=32)
     cpu_s = time.perf_counter() - t0
@@ -555,6 +563,7 @@ def bench_composite(dev, n_images=8, size=1024, cover=0.8, reps=10) -> dict:
             "bit_identical_to_reference_order_f32": exact,
             "caller_range_ms": async_ms, "caller_range_bit_identical": async_exact,
             "caller_range_roofline_frac": alg / (async_ms / 1e3) / 1e9 / peaks()["hbm_gbs"],
+            "caller_range_c_abi_ms": cabi_ms,
             "cpu_oracle_ms": cpu_s * 1e3, "cpu_oracle_kind": "oracle C compositor (qsort, 1 thread)",
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": pk["hbm_gbs"],
                          "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / pk["hbm_gbs"],

@@ -109,5 +109,5 @@ def test_gradient_descent_step_reduces_loss():
         loss = ((img - target) ** 2).sum()
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     assert losses[-1] < losses[0]
