@@ -146,12 +146,14 @@ __global__ void range_kernel(const Partial *__restrict__ in, int64_t n, unsigned
   }
 }
 
-// cnt[p] = records of pixel lo + p; rank[i] = record i's slot in its bucket
-// (in arrival order; the emit kernel restores input order). A record whose
-// id lies outside [lo, lo + r) (possible only when the caller gave the
-// range) is left out and sets *bad.
+// cnt[p] = records of pixel lo + p; pr[i] = {p, record i's slot in its
+// bucket} (slots in arrival order; the emit kernel restores input order),
+// so that the bucket pass reads 8 bytes per record instead of the 24-byte
+// records again. A record whose id lies outside [lo, lo + r) (possible only
+// when the caller gave the range) is left out (p = 0xffffffff) and sets
+// *bad.
 __global__ void count_kernel(const Partial *__restrict__ in, int64_t n, int lo, int64_t r,
-                             uint32_t *__restrict__ cnt, uint32_t *__restrict__ rank,
+                             uint32_t *__restrict__ cnt, uint2 *__restrict__ pr,
                              unsigned *__restrict__ bad)
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -159,21 +161,21 @@ __global__ void count_kernel(const Partial *__restrict__ in, int64_t n, int lo, 
     const int64_t p = (int64_t)in[i].pixel_id - lo;
     if (p < 0 || p >= r) {
       atomicOr(bad, 1u);
+      pr[i] = make_uint2(0xffffffffu, 0u);
       continue;
     }
-    rank[i] = atomicAdd(cnt + p, 1u);
+    pr[i] = make_uint2((uint32_t)p, atomicAdd(cnt + p, 1u));
   }
 }
 
-__global__ void bucket_kernel(const Partial *__restrict__ in, int64_t n, int lo, int64_t r,
-                              const uint32_t *__restrict__ off, const uint32_t *__restrict__ rank,
-                              uint32_t *__restrict__ order)
+__global__ void bucket_kernel(const uint2 *__restrict__ pr, int64_t n, int64_t r,
+                              const uint32_t *__restrict__ off, uint32_t *__restrict__ order)
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = (int64_t)in[i].pixel_id - lo;
-    if (p < 0 || p >= r) continue;
-    order[off[p] + rank[i]] = (uint32_t)i;
+    const uint2 v = pr[i];
+    if ((int64_t)v.x >= r) continue;
+    order[off[v.x] + v.y] = (uint32_t)i;
   }
 }
 
@@ -402,7 +404,7 @@ struct Arena {
 
 size_t dense_bytes(int64_t n, int64_t r)
 {
-  return 256 * 9 + (4 * (size_t)r + 2 * (size_t)n + std::max<size_t>(scan_scratch_words(r), 3 * 1024) + 3) *
+  return 256 * 9 + (4 * (size_t)r + 3 * (size_t)n + std::max<size_t>(scan_scratch_words(r), 3 * 1024) + 3) *
                        sizeof(uint32_t);
 }
 
@@ -418,11 +420,12 @@ cudaError_t composite_dense(const Partial *in, int64_t n, int lo, int64_t r, Par
 {
   uint32_t *cnt = a.take<uint32_t>(r), *off = a.take<uint32_t>(r);
   uint32_t *upos = a.take<uint32_t>(r), *mpos = a.take<uint32_t>(r);
-  uint32_t *rank = a.take<uint32_t>(n), *order = a.take<uint32_t>(n);
+  uint2 *pr = a.take<uint2>(n);
+  uint32_t *order = a.take<uint32_t>(n);
   uint32_t *scan_tmp = a.take<uint32_t>(std::max<size_t>(scan_scratch_words(r), 3 * (size_t)kTile3));
   cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * r, st);
   if (e != cudaSuccess) return e;
-  count_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, cnt, rank, bad);
+  count_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, cnt, pr, bad);
   count_launch();
   const int64_t tiles = (r + kTile3 - 1) / kTile3;
   if (tiles <= kTile3) {
@@ -443,7 +446,7 @@ cudaError_t composite_dense(const Partial *in, int64_t n, int lo, int64_t r, Par
     if ((e = exclusive_scan(upos, r, scan_tmp, st)) != cudaSuccess) return e;
     if ((e = exclusive_scan(mpos, r, scan_tmp, st)) != cudaSuccess) return e;
   }
-  bucket_kernel<<<grid_of(n), 256, 0, st>>>(in, n, lo, r, off, rank, order);
+  bucket_kernel<<<grid_of(n), 256, 0, st>>>(pr, n, r, off, order);
   count_launch();
   pixel_emit_kernel<<<grid_of(r), 256, 0, st>>>(in, cnt, off, upos, mpos, order, r, out, totals);
   count_launch();
