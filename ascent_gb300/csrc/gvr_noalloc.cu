@@ -110,6 +110,11 @@ noalloc_march(const Grid g, const ViewDev view, const MarchParams mp,
       const int64_t sy = g.dims[0], sz = (int64_t)g.dims[0] * g.dims[1];
       const float thr = mp.early_term < 1.f ? mp.early_term : 2.f;
       const float nm1 = (float)(mp.lut_size - 1);
+      // a sample in the cell of the sample before keeps that cell's corners
+      // (the scene march does the same; the values, and so the image, are
+      // unchanged)
+      int64_t last = -1;
+      float lc[8];
       for (int k = 0;; ++k) {
         const float t = fmaf((float)k, mp.sample_dist, t0);
         if (!(t < t1)) break;
@@ -121,11 +126,23 @@ noalloc_march(const Grid g, const ViewDev view, const MarchParams mp,
           c[a] = max(0, min((int)gg, g.dims[a] - 2));
           w[a] = gg - (float)c[a];
         }
-        const float *p = g.field + (c[2] * sz + (int64_t)c[1] * sy + c[0]);
-        const float c00 = lerp1(__ldg(p), __ldg(p + 1), w[0]);
-        const float c10 = lerp1(__ldg(p + sy), __ldg(p + sy + 1), w[0]);
-        const float c01 = lerp1(__ldg(p + sz), __ldg(p + sz + 1), w[0]);
-        const float c11 = lerp1(__ldg(p + sz + sy), __ldg(p + sz + sy + 1), w[0]);
+        const int64_t off = c[2] * sz + (int64_t)c[1] * sy + c[0];
+        if (off != last) {
+          const float *p = g.field + off;
+          lc[0] = __ldg(p);
+          lc[1] = __ldg(p + 1);
+          lc[2] = __ldg(p + sy);
+          lc[3] = __ldg(p + sy + 1);
+          lc[4] = __ldg(p + sz);
+          lc[5] = __ldg(p + sz + 1);
+          lc[6] = __ldg(p + sz + sy);
+          lc[7] = __ldg(p + sz + sy + 1);
+          last = off;
+        }
+        const float c00 = lerp1(lc[0], lc[1], w[0]);
+        const float c10 = lerp1(lc[2], lc[3], w[0]);
+        const float c01 = lerp1(lc[4], lc[5], w[0]);
+        const float c11 = lerp1(lc[6], lc[7], w[0]);
         const float v = lerp1(lerp1(c00, c10, w[1]), lerp1(c01, c11, w[1]), w[2]);
         const float s = __saturatef((v - mp.scalar_min) * mp.inv_range);
         float4 col;

@@ -64,7 +64,7 @@ def parse_args():
                     help="skip the ingest, plain-64, hex, batched, differentiable and compositing configurations")
     ap.add_argument("--configs", default="",
                     help="comma-separated subset of ingest,plain_64,hex,batched,differentiable,composite,"
-                         "zbuffer (default: all)")
+                         "zbuffer,noalloc (default: all)")
     ap.add_argument("--staging", choices=["auto", "off", "on"], default="auto",
                     help="plain path: let the tuner choose between L1 gathers and shared-memory brick "
                          "staging (auto), or time only one of them")
@@ -570,6 +570,65 @@ def bench_composite(dev, n_images=8, size=1024, cover=0.8, reps=10) -> dict:
                          "bytes_per_record": "24 read + 24 per output record"}}
 
 
+def bench_noalloc(dev, n_cells=512, size=1024, reps=10) -> dict:
+    """gvr_render_uniform_noalloc (no device allocation; the caller's field
+    read in its plain node layout) on the benchmark's 513^3 field as one
+    domain at 1024^2, beside gvr_render_volume on a scene holding the same
+    domain in bricks; both through the C ABI with prebuilt arguments. The
+    two images are compared with each other over the whole frame."""
+    import ctypes as C
+    import torch
+    from ascent_gb300 import _native as N
+    from ascent_gb300 import scene as S
+    from ascent_gb300 import volume as V
+    W = workloads_module()
+    wl = W.plain_large(n_cells=n_cells, width=size, height=size, parts=(1, 1, 1))
+    d = wl.domains[0]
+    cam = V.workload_camera(wl)
+    p = V.workload_params(wl)
+    stream = torch.cuda.current_stream(dev)
+    field = torch.from_numpy(d.field).cuda(dev)
+    rgba = torch.empty((size, size, 4), dtype=torch.float32, device=f"cuda:{dev}")
+    depth = torch.empty((size, size), dtype=torch.float32, device=f"cuda:{dev}")
+    fn = N.lib().gvr_render_uniform_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                   C.POINTER(N.Camera), C.POINTER(N.RenderParams), C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.POINTER(C.c_uint64)]
+    dims = (C.c_int * 3)(*d.dims)
+    origin = (C.c_double * 3)(*d.origin)
+    spacing = (C.c_double * 3)(*d.spacing)
+    args = (C.c_void_p(field.data_ptr()), dims, origin, spacing, C.byref(cam), C.byref(p),
+            C.c_void_p(rgba.data_ptr()), C.c_void_p(depth.data_ptr()), C.c_void_p(stream.cuda_stream))
+    n = C.c_uint64(0)
+    if fn(*args, C.byref(n)) != 0:
+        raise RuntimeError(N.lib().gvr_last_error())
+    samples = int(n.value)
+
+    def call():
+        if fn(*args, None) != 0:
+            raise RuntimeError(N.lib().gvr_last_error())
+    for _ in range(3):
+        call()
+    ms = _timed(call, stream, reps)
+    na_img = rgba.cpu().numpy()
+    with S.Scene(dev) as sc:
+        sc.add_uniform(d.field, d.origin, d.spacing)
+        sargs = (sc.handle, C.byref(cam), C.byref(p), C.c_void_p(rgba.data_ptr()),
+                 C.c_void_p(depth.data_ptr()), N.MEM_DEVICE, C.c_void_p(stream.cuda_stream), None)
+        for _ in range(3):
+            N.call("gvr_render_volume", *sargs)
+        scene_ms = _timed(lambda: N.call("gvr_render_volume", *sargs), stream, reps)
+        sc_img = rgba.cpu().numpy()
+    err = np.abs(na_img.astype(np.float64) - sc_img)
+    del field
+    return {"workload": f"noalloc uniform{n_cells}^3x1dom@{size}x{size}", "samples_per_frame": samples,
+            "ms_per_frame": ms, "gsamples_per_s": samples / ms / 1e6,
+            "scene_path_ms_per_frame": scene_ms, "scene_path_gsamples_per_s": samples / scene_ms / 1e6,
+            "vs_scene_path": {"max": float(err.max()),
+                              "frac_within_2_255": float((err <= 2 / 255 + 1e-7).all(axis=-1).mean())}}
+
+
 def bench_zbuffer(dev, n_images=4, size=1024, reps=20) -> dict:
     """Z-buffer compositing of n_images opaque 1024^2 canvases (RGBA float +
     depth, device memory; seeded colours, depths uniform in [0, 1.2] so that
@@ -919,7 +978,7 @@ def run_ours(args):
         runs = {"ingest": lambda: bench_ingest(dev, wl), "plain_64": lambda: bench_plain_small(dev),
                 "hex": lambda: bench_hex(dev), "batched": lambda: bench_batch(dev),
                 "differentiable": lambda: bench_diff(dev), "composite": lambda: bench_composite(dev),
-                "zbuffer": lambda: bench_zbuffer(dev)}
+                "zbuffer": lambda: bench_zbuffer(dev), "noalloc": lambda: bench_noalloc(dev)}
         for name in (args.configs.split(",") if args.configs else runs):
             others[name] = runs[name]()
     line = {
