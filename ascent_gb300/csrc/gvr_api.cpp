@@ -1222,14 +1222,21 @@ static int render_one(gvr_scene *s, const gvr_camera *camera, const gvr_render_p
                           ((p->height + kMarchTile - 1) / kMarchTile);
   if (s->tuning.tile_order == 1 && n_tiles <= kCostOrderTiles) {
     if (s->cost_order_cap < n_tiles) {
+      // order, costs, and the costs' maximum (zeroed here, then by every
+      // sort launch)
+      if (s->d_cost_order && (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return cuda_error(e, "tile cost order");
       cudaFree(s->d_cost_order);
       s->d_cost_order = nullptr;
       s->cost_order_cap = 0;
-      e = cudaMalloc(&s->d_cost_order, sizeof(int) * n_tiles);
+      e = cudaMalloc(&s->d_cost_order, sizeof(int) * (2 * n_tiles + 1));
+      if (e == cudaSuccess) e = cudaMemsetAsync(s->d_cost_order + 2 * n_tiles, 0, sizeof(int), st);
       if (e != cudaSuccess) return cuda_error(e, "cudaMalloc tile cost order");
       s->cost_order_cap = n_tiles;
     }
-    e = launch_tile_cost_order(s->d_domains, view, mp, s->d_cost_order, st);
+    e = launch_tile_cost_order(s->d_domains, view, mp, s->d_cost_order,
+                               reinterpret_cast<unsigned *>(s->d_cost_order + s->cost_order_cap),
+                               reinterpret_cast<unsigned *>(s->d_cost_order + 2 * s->cost_order_cap), st);
     if (e != cudaSuccess) return cuda_error(e, "tile cost order launch");
     d_order = s->d_cost_order;
   } else if ((rc = tile_order(s, p->width, p->height, &d_order)) != GVR_OK) {

@@ -217,7 +217,8 @@ struct gvr_scene {
   // indices, nearest the image centre first); written once, then read only
   std::map<std::pair<int, int>, int *> tile_orders;
   // per-view longest-first tile order (tile_order 1), rewritten by every
-  // render that uses it
+  // render that uses it: the order (cap ints), the tile costs (cap words)
+  // and the costs' maximum (one word, 0 between renders)
   int *d_cost_order = nullptr;
   int64_t cost_order_cap = 0;
 };
@@ -298,11 +299,12 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
                          unsigned long long *d_samples, const Tuning &tuning,
                          bool has_hex, const int *d_order, cudaStream_t stream);
 // longest-first tile order for one view (gvr_march.cu): writes a permutation
-// of the view's kMarchTile tiles to d_order (one int per tile); grids of more
-// than kCostOrderTiles tiles are refused (cudaErrorInvalidValue)
+// of the view's kMarchTile tiles to d_order (one int per tile); d_keys holds
+// one word per tile of scratch and *d_top a word that is 0 between calls;
+// grids of more than kCostOrderTiles tiles are refused (cudaErrorInvalidValue)
 constexpr int kCostOrderTiles = 48 * 1024;
 cudaError_t launch_tile_cost_order(const DomainDev *d_domains, const ViewDev &view, const MarchParams &mp,
-                                   int *d_order, cudaStream_t stream);
+                                   int *d_order, unsigned *d_keys, unsigned *d_top, cudaStream_t stream);
 // staged march (gvr_march.cu): uniform vertex-field domains only, taken in
 // `order`; *d_stage_fail counts CTAs whose bounded wait for their bulk
 // copies gave up (they finish from global memory)

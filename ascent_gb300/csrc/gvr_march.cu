@@ -1524,24 +1524,21 @@ cudaError_t launch_march(const DomainDev *d_domains, const ViewDev &view,
 // tile is the summed length, through every domain box, of five of its rays
 // (its centre and corner pixels); tiles are counting-sorted into 1024 cost
 // bins, longest first, so that the last tiles the GPU takes are the short
-// ones (longest-processing-time-first list scheduling). One CTA; the order
-// of tiles within a bin is whatever the shared-memory atomics give, and no
-// order changes a pixel. Dynamic shared memory: one int per tile.
-__global__ void __launch_bounds__(1024)
-tile_cost_order_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ ViewDev view,
-                       const __grid_constant__ MarchParams mp, int *__restrict__ order)
+// ones (longest-processing-time-first list scheduling). Two launches: the
+// costs with one thread per tile (keys[t] = the cost's bits, *top = their
+// maximum), then one CTA bins, scans and scatters them and clears *top for
+// the next view. The order of tiles within a bin is whatever the
+// shared-memory atomics give, and no order changes a pixel.
+__global__ void __launch_bounds__(256)
+tile_cost_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ ViewDev view,
+                 const __grid_constant__ MarchParams mp, unsigned *__restrict__ keys,
+                 unsigned *__restrict__ top)
 {
-  extern __shared__ int s_key[];
-  __shared__ int s_hist[1024];
-  __shared__ int s_warp[32];
-  __shared__ unsigned s_max;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int tiles_x = (mp.width + kTile - 1) / kTile;
   const int n = tiles_x * ((mp.height + kTile - 1) / kTile);
-  s_hist[tid] = 0;
-  if (tid == 0) s_max = 0u;
-  __syncthreads();
-  for (int t = tid; t < n; t += 1024) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned bits = 0u;
+  if (t < n) {
     const int x0 = (t % tiles_x) * kTile, y0 = (t / tiles_x) * kTile;
     const int x1 = min(x0 + kTile - 1, mp.width - 1), y1 = min(y0 + kTile - 1, mp.height - 1);
     const int rx[5] = {(x0 + x1) >> 1, x0, x1, x0, x1};
@@ -1555,17 +1552,28 @@ tile_cost_order_kernel(const DomainDev *__restrict__ g_domains, const __grid_con
       }
     }
     cost = cost > 0.f && cost < FLT_MAX ? cost : 0.f;   // NaN and inf cost nothing
-    s_key[t] = __float_as_int(cost);
-    atomicMax(&s_max, __float_as_uint(cost));
+    bits = __float_as_uint(cost);
+    keys[t] = bits;
   }
+  bits = __reduce_max_sync(0xffffffffu, bits);
+  if ((threadIdx.x & 31) == 0 && bits) atomicMax(top, bits);
+}
+
+__global__ void __launch_bounds__(1024)
+tile_order_sort_kernel(const __grid_constant__ MarchParams mp, const unsigned *__restrict__ keys,
+                       unsigned *__restrict__ top, int *__restrict__ order)
+{
+  __shared__ int s_hist[1024];
+  __shared__ int s_warp[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tiles_x = (mp.width + kTile - 1) / kTile;
+  const int n = tiles_x * ((mp.height + kTile - 1) / kTile);
+  s_hist[tid] = 0;
+  const float high = __uint_as_float(*top);
+  const float scale = high > 0.f ? 1023.f / high : 0.f;
   __syncthreads();
-  const float top = __uint_as_float(s_max);
-  const float scale = top > 0.f ? 1023.f / top : 0.f;
-  for (int t = tid; t < n; t += 1024) {
-    const int k = 1023 - min(1023, (int)(__int_as_float(s_key[t]) * scale));
-    s_key[t] = k;
-    atomicAdd(&s_hist[k], 1);
-  }
+  for (int t = tid; t < n; t += 1024)
+    atomicAdd(&s_hist[1023 - min(1023, (int)(__uint_as_float(keys[t]) * scale))], 1);
   __syncthreads();
   // exclusive scan of the 1024 bins, one per thread
   const int v = s_hist[tid];
@@ -1589,20 +1597,21 @@ tile_cost_order_kernel(const DomainDev *__restrict__ g_domains, const __grid_con
   __syncthreads();
   s_hist[tid] = x - v + (warp ? s_warp[warp - 1] : 0);
   __syncthreads();
-  for (int t = tid; t < n; t += 1024) order[atomicAdd(&s_hist[s_key[t]], 1)] = t;
+  for (int t = tid; t < n; t += 1024) {
+    const int bin = 1023 - min(1023, (int)(__uint_as_float(keys[t]) * scale));
+    order[atomicAdd(&s_hist[bin], 1)] = t;
+  }
+  if (tid == 0) *top = 0u;
 }
 
 cudaError_t launch_tile_cost_order(const DomainDev *d_domains, const ViewDev &view, const MarchParams &mp,
-                                   int *d_order, cudaStream_t stream)
+                                   int *d_order, unsigned *d_keys, unsigned *d_top, cudaStream_t stream)
 {
   const int64_t tiles = (int64_t)((mp.width + kTile - 1) / kTile) * ((mp.height + kTile - 1) / kTile);
   if (tiles > kCostOrderTiles) return cudaErrorInvalidValue;
-  const size_t smem = sizeof(int) * (size_t)tiles;
-  cudaError_t e = cudaFuncSetAttribute(tile_cost_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(sizeof(int) * kCostOrderTiles));
-  if (e != cudaSuccess) return e;
-  tile_cost_order_kernel<<<1, 1024, smem, stream>>>(d_domains, view, mp, d_order);
-  count_launch();
+  tile_cost_kernel<<<(unsigned)((tiles + 255) / 256), 256, 0, stream>>>(d_domains, view, mp, d_keys, d_top);
+  tile_order_sort_kernel<<<1, 1024, 0, stream>>>(mp, d_keys, d_top, d_order);
+  count_launch(2);
   return cudaGetLastError();
 }
 
