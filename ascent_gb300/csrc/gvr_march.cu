@@ -213,6 +213,59 @@ __device__ __noinline__ Partial march_domain(const DomainDev &dm, const Ray r, f
 }
 
 
+// Samples k .. k + UNROLL - 1 of a ray in a uniform vertex domain, whose
+// grid-space position at distance t is A + t B: each is located, its cell's
+// 8 corners are loaded from the bricks unless the sample before was in the
+// same cell (lc, last_off hold that cell's), and v[u] is the trilinear
+// value. ok[u]: the sample lies before t1 (and, with LIMIT, its index
+// before kend); a sample that does not is placed at t0 so that its loads
+// stay inside the domain. Shared by the per-domain loops and the one-loop
+// domain walk, so all of them take the same samples with the same
+// arithmetic.
+template <int UNROLL, int SH, bool LIMIT>
+__device__ __forceinline__ void sample_cells(const float *__restrict__ bricks, const float A[3],
+                                             const float B[3], const int cmax[3], int sy, int sz,
+                                             int k, int kend, float dt, float t0, float t1,
+                                             int &last_off, float lc[8], float v[UNROLL],
+                                             bool ok[UNROLL])
+{
+  constexpr int BC = brick_cells(SH), BN = brick_nodes(SH), BF = brick_floats(SH);
+#pragma unroll
+  for (int u = 0; u < UNROLL; ++u) {
+    float t = fmaf((float)(k + u), dt, t0);
+    ok[u] = LIMIT ? (k + u < kend && t < t1) : t < t1;
+    t = ok[u] ? t : t0;
+    int off = 0;
+    float w[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float g = fmaf(t, B[a], A[a]);
+      const int c = max(0, min((int)g, cmax[a]));
+      w[a] = g - (float)c;
+      const int hi = c >> SH, lo = c & (BC - 1);
+      off += a == 0 ? hi * BF + lo
+                    : (a == 1 ? hi * sy + lo * BN : hi * sz + lo * BN * BN);
+    }
+    if (off != last_off) {
+      const float *p = bricks + off;
+      lc[0] = __ldg(p);
+      lc[1] = __ldg(p + 1);
+      lc[2] = __ldg(p + BN);
+      lc[3] = __ldg(p + BN + 1);
+      lc[4] = __ldg(p + BN * BN);
+      lc[5] = __ldg(p + BN * BN + 1);
+      lc[6] = __ldg(p + BN * BN + BN);
+      lc[7] = __ldg(p + BN * BN + BN + 1);
+      last_off = off;
+    }
+    const float c00 = lerpf(lc[0], lc[1], w[0]);
+    const float c10 = lerpf(lc[2], lc[3], w[0]);
+    const float c01 = lerpf(lc[4], lc[5], w[0]);
+    const float c11 = lerpf(lc[6], lc[7], w[0]);
+    v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
+  }
+}
+
 // Uniform grid, vertex field, no empty bricks: the hot path. UNROLL samples
 // are located and their 8 corners loaded before any of them is blended, so
 // a warp keeps UNROLL x 8 loads in flight. A sample in the cell of the one
@@ -245,40 +298,7 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
   for (int k = 0;; k += UNROLL) {
     float v[UNROLL];
     bool ok[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      float t = fmaf((float)(k + u), dt, t0);
-      ok[u] = t < t1;
-      t = ok[u] ? t : t0;
-      int off = 0;
-      float w[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float g = fmaf(t, B[a], A[a]);
-        const int c = max(0, min((int)g, cmax[a]));
-        w[a] = g - (float)c;
-        const int hi = c >> SH, lo = c & (BC - 1);
-        off += a == 0 ? hi * BF + lo
-                      : (a == 1 ? hi * sy + lo * BN : hi * sz + lo * BN * BN);
-      }
-      if (off != last_off) {
-        const float *p = bricks + off;
-        lc[0] = __ldg(p);
-        lc[1] = __ldg(p + 1);
-        lc[2] = __ldg(p + BN);
-        lc[3] = __ldg(p + BN + 1);
-        lc[4] = __ldg(p + BN * BN);
-        lc[5] = __ldg(p + BN * BN + 1);
-        lc[6] = __ldg(p + BN * BN + BN);
-        lc[7] = __ldg(p + BN * BN + BN + 1);
-        last_off = off;
-      }
-      const float c00 = lerpf(lc[0], lc[1], w[0]);
-      const float c10 = lerpf(lc[2], lc[3], w[0]);
-      const float c01 = lerpf(lc[4], lc[5], w[0]);
-      const float c11 = lerpf(lc[6], lc[7], w[0]);
-      v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
-    }
+    sample_cells<UNROLL, SH, false>(bricks, A, B, cmax, sy, sz, k, 0, dt, t0, t1, last_off, lc, v, ok);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       if (!ok[u]) return count;
@@ -355,40 +375,7 @@ __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, f
     for (; k < kend; k += UNROLL) {
       float v[UNROLL];
       bool ok[UNROLL];
-#pragma unroll
-      for (int u = 0; u < UNROLL; ++u) {
-        float ts = fmaf((float)(k + u), dt, t0);
-        ok[u] = k + u < kend && ts < t1;
-        ts = ok[u] ? ts : t0;
-        int off = 0;
-        float w[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const float g = fmaf(ts, B[a], A[a]);
-          const int c = max(0, min((int)g, cmax[a]));
-          w[a] = g - (float)c;
-          const int hi = c >> SH, lo = c & (BC - 1);
-          off += a == 0 ? hi * BF + lo
-                        : (a == 1 ? hi * sy + lo * BN : hi * sz + lo * BN * BN);
-        }
-        if (off != last_off) {
-          const float *p = bricks + off;
-          lc[0] = __ldg(p);
-          lc[1] = __ldg(p + 1);
-          lc[2] = __ldg(p + BN);
-          lc[3] = __ldg(p + BN + 1);
-          lc[4] = __ldg(p + BN * BN);
-          lc[5] = __ldg(p + BN * BN + 1);
-          lc[6] = __ldg(p + BN * BN + BN);
-          lc[7] = __ldg(p + BN * BN + BN + 1);
-          last_off = off;
-        }
-        const float c00 = lerpf(lc[0], lc[1], w[0]);
-        const float c10 = lerpf(lc[2], lc[3], w[0]);
-        const float c01 = lerpf(lc[4], lc[5], w[0]);
-        const float c11 = lerpf(lc[6], lc[7], w[0]);
-        v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
-      }
+      sample_cells<UNROLL, SH, true>(bricks, A, B, cmax, sy, sz, k, kend, dt, t0, t1, last_off, lc, v, ok);
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         if (!ok[u]) break;
@@ -731,40 +718,7 @@ __device__ __forceinline__ int render_ray_unified(const DomainDev *doms, uint64_
     }
     float v[UNROLL];
     bool ok[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      float t = fmaf((float)(k + u), dt, bt0);
-      ok[u] = t < bt1;
-      t = ok[u] ? t : bt0;
-      int off = 0;
-      float w[3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float g = fmaf(t, B[a], A[a]);
-        const int c = max(0, min((int)g, cmax[a]));
-        w[a] = g - (float)c;
-        const int hi = c >> SH, lo = c & (BC - 1);
-        off += a == 0 ? hi * BF + lo
-                      : (a == 1 ? hi * sy + lo * BN : hi * sz + lo * BN * BN);
-      }
-      if (off != last_off) {
-        const float *p = bricks + off;
-        lc[0] = __ldg(p);
-        lc[1] = __ldg(p + 1);
-        lc[2] = __ldg(p + BN);
-        lc[3] = __ldg(p + BN + 1);
-        lc[4] = __ldg(p + BN * BN);
-        lc[5] = __ldg(p + BN * BN + 1);
-        lc[6] = __ldg(p + BN * BN + BN);
-        lc[7] = __ldg(p + BN * BN + BN + 1);
-        last_off = off;
-      }
-      const float c00 = lerpf(lc[0], lc[1], w[0]);
-      const float c10 = lerpf(lc[2], lc[3], w[0]);
-      const float c01 = lerpf(lc[4], lc[5], w[0]);
-      const float c11 = lerpf(lc[6], lc[7], w[0]);
-      v[u] = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
-    }
+    sample_cells<UNROLL, SH, false>(bricks, A, B, cmax, sy, sz, k, 0, dt, bt0, bt1, last_off, lc, v, ok);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
       if (!ok[u]) { fresh = true; break; }
