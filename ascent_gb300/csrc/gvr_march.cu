@@ -290,19 +290,19 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
   const int sz = dm.nbrick[1] * sy;
   const float *__restrict__ bricks = dm.bricks;
   const float nm1 = (float)(mp.lut_size - 1);
-  int count = 0;
   // corners of the last cell loaded (at half-cell spacing about half of the
   // samples fall in the cell of the sample before)
   int last_off = -1;
   float lc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  // samples taken: k + u when sample k + u lies past t1, k + u + 1 when it
+  // reached the threshold (no counter in the loop)
   for (int k = 0;; k += UNROLL) {
     float v[UNROLL];
     bool ok[UNROLL];
     sample_cells<UNROLL, SH, false>(bricks, A, B, cmax, sy, sz, k, 0, dt, t0, t1, last_off, lc, v, ok);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      if (!ok[u]) return count;
-      ++count;
+      if (!ok[u]) return k + u;
       const float s = __saturatef((v[u] - mp.scalar_min) * mp.inv_range);
       float4 col;
       if (mp.lut_filter == GVR_LUT_LINEAR) {
@@ -315,7 +315,7 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
       acc.y = fmaf(wa, col.y, acc.y);
       acc.z = fmaf(wa, col.z, acc.z);
       acc.w += wa;
-      if (acc.w >= thr) return count;
+      if (acc.w >= thr) return k + u + 1;
     }
   }
 }
@@ -721,8 +721,7 @@ __device__ __forceinline__ int render_ray_unified(const DomainDev *doms, uint64_
     sample_cells<UNROLL, SH, false>(bricks, A, B, cmax, sy, sz, k, 0, dt, bt0, bt1, last_off, lc, v, ok);
 #pragma unroll
     for (int u = 0; u < UNROLL; ++u) {
-      if (!ok[u]) { fresh = true; break; }
-      ++count;
+      if (!ok[u]) { count += k + u; fresh = true; break; }
       const float sc = __saturatef((v[u] - mp.scalar_min) * mp.inv_range);
       float4 col;
       if (mp.lut_filter == GVR_LUT_LINEAR) {
@@ -735,7 +734,7 @@ __device__ __forceinline__ int render_ray_unified(const DomainDev *doms, uint64_
       acc.y = fmaf(wa, col.y, acc.y);
       acc.z = fmaf(wa, col.z, acc.z);
       acc.w += wa;
-      if (acc.w >= thr) { fresh = true; break; }
+      if (acc.w >= thr) { count += k + u + 1; fresh = true; break; }
     }
     k += UNROLL;
   }
