@@ -66,6 +66,14 @@ __device__ __forceinline__ float lerpf(float a, float b, float w)
   return fmaf(w, b - a, a);
 }
 
+// Nearest LUT entry of a saturated scalar s in [0, 1]: s * (n - 1) <= n - 1
+// in float, so (int)(s * nm1) is an index of the table without a clamp
+// (the value a clamp to n - 1 would give).
+__device__ __forceinline__ float4 lut_nearest(const float4 *lut, float nm1, float s)
+{
+  return lut[(int)(s * nm1)];
+}
+
 __device__ __forceinline__ float4 lut_fetch(const float4 *lut, int n, int filter, float s)
 {
   if (filter == GVR_LUT_LINEAR) {
@@ -308,7 +316,7 @@ __device__ __forceinline__ int march_uniform(const DomainDev &dm, const Ray &r, 
       if (mp.lut_filter == GVR_LUT_LINEAR) {
         col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, s);
       } else {
-        col = lut[min((int)(s * nm1), mp.lut_size - 1)];
+        col = lut_nearest(lut, nm1, s);
       }
       const float wa = (1.f - acc.w) * col.w;
       acc.x = fmaf(wa, col.x, acc.x);
@@ -385,7 +393,7 @@ __device__ __forceinline__ int march_bricks(const DomainDev &dm, const Ray &r, f
         if (mp.lut_filter == GVR_LUT_LINEAR) {
           col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, sc);
         } else {
-          col = lut[min((int)(sc * nm1), mp.lut_size - 1)];
+          col = lut_nearest(lut, nm1, sc);
         }
         const float wa = (1.f - acc.w) * col.w;
         acc.x = fmaf(wa, col.x, acc.x);
@@ -727,7 +735,7 @@ __device__ __forceinline__ int render_ray_unified(const DomainDev *doms, uint64_
       if (mp.lut_filter == GVR_LUT_LINEAR) {
         col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, sc);
       } else {
-        col = lut[min((int)(sc * nm1), mp.lut_size - 1)];
+        col = lut_nearest(lut, nm1, sc);
       }
       const float wa = (1.f - acc.w) * col.w;
       acc.x = fmaf(wa, col.x, acc.x);
@@ -1286,7 +1294,7 @@ staged_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ V
         if (mp.lut_filter == GVR_LUT_LINEAR) {
           col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, sc);
         } else {
-          col = lut[min((int)(sc * nm1), mp.lut_size - 1)];
+          col = lut_nearest(lut, nm1, sc);
         }
         const float wa = (1.f - acc.w) * col.w;
         acc.x = fmaf(wa, col.x, acc.x);
