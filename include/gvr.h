@@ -306,9 +306,9 @@ GVR_API int gvr_scene_set_staging(gvr_scene *scene, int mode);
 
 /* Launch order of the plain march's 16 x 16 tiles: mode 0 (default) takes
  * the tiles nearest the image centre first, from a table built once per
- * image size; mode 1 runs, before every render, one small kernel that
- * estimates each tile's cost for that view (the length of five of its rays
- * inside the domain boxes) and launches the longest tiles first. Images are
+ * image size; mode 1 runs, before every render, two small kernels that
+ * estimate each tile's cost for that view (the length of five of its rays
+ * inside the domain boxes) and sort the tiles, longest first. Images are
  * the same either way. Renders of one scene share the mode-1 order buffer,
  * like its transfer-function state: do not overlap them on different
  * streams. Set by the autotuner; no counterpart in the reference. */
