@@ -1137,7 +1137,7 @@ int gvr_scene_set_brick_cells(gvr_scene *s, int cells)
 int gvr_scene_set_staging(gvr_scene *s, int mode)
 {
   if (!s) return set_error(GVR_ERR_INVALID_ARGUMENT, "scene is NULL");
-  if (mode != 0 && mode != 1) return set_error(GVR_ERR_INVALID_ARGUMENT, "staging mode must be 0 or 1");
+  if (mode < 0 || mode > 2) return set_error(GVR_ERR_INVALID_ARGUMENT, "staging mode must be 0, 1 or 2");
   s->tuning.staged = mode;
   return GVR_OK;
 }

@@ -1338,6 +1338,381 @@ staged_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ V
 }
 
 
+// ---------------------------------------------------------------------------
+// Layer-staged march (staging mode 2): uniform vertex domains in 8^3-cell
+// bricks, walked by brick layers along the axis the tile's rays advance
+// fastest on. For each layer the tile's four corner rays, crossing the
+// layer's two bounding planes, give a window of bricks that holds every
+// sample the tile's rays take in that layer (the rays of the tile lie in the
+// cone of its corner rays); the window's bricks are bulk-copied
+// (cp.async.bulk, 2944 contiguous bytes each) into one of two shared-memory
+// buffers, the next layer's copies in flight while the rays sample the
+// current one. A window larger than SLOTS bricks, a layer that contains the
+// camera, a sample outside the window (rounding) and a CTA whose bounded
+// wait gave up read global memory instead: the same values, so images
+// equal the gather march's. Domains are taken in one front-to-back order per
+// CTA, as in staged_kernel. A scene with empty bricks to jump, or any domain
+// this walk does not cover, is rendered by render_ray for every pixel.
+// ---------------------------------------------------------------------------
+constexpr long long kLayerPolls = 1 << 20;
+
+// Thread 0: the window of layer L into win[0..3] = {first u brick, first v
+// brick, width, height} (win[0] = -1: not staged) and its bulk copies into
+// buf, completing on bar.
+template <int SLOTS>
+__device__ void layer_issue(const DomainDev &dm, const float (*cA)[3], const float (*cB)[3], int ax, int L,
+                           float *buf, uint64_t *bar, int *win)
+{
+  const int u = ax == 0 ? 1 : 0, v = ax == 2 ? 1 : 2;
+  float lo_u = FLT_MAX, hi_u = -FLT_MAX, lo_v = FLT_MAX, hi_v = -FLT_MAX;
+  bool ok = true;
+  for (int c = 0; c < 4; ++c) {
+    if (!(cB[c][ax] != 0.f)) { ok = false; break; }
+    for (int q = 0; q < 2; ++q) {
+      const float t = ((float)((L + q) * kBrickCells) - cA[c][ax]) / cB[c][ax];
+      if (!(t >= 0.f)) ok = false;   // the layer holds the camera (or NaN)
+      const float gu = fmaf(t, cB[c][u], cA[c][u]), gv = fmaf(t, cB[c][v], cA[c][v]);
+      lo_u = fminf(lo_u, gu); hi_u = fmaxf(hi_u, gu);
+      lo_v = fminf(lo_v, gv); hi_v = fmaxf(hi_v, gv);
+    }
+  }
+  int bu0 = 0, bu1 = -1, bv0 = 0, bv1 = -1;
+  if (ok && lo_u > -1e9f && hi_u < 1e9f && lo_v > -1e9f && hi_v < 1e9f) {
+    const int cu = dm.dims[u] - 2, cv = dm.dims[v] - 2;
+    bu0 = max(0, min((int)floorf(lo_u), cu)) >> 3;
+    bu1 = max(0, min((int)floorf(hi_u), cu)) >> 3;
+    bv0 = max(0, min((int)floorf(lo_v), cv)) >> 3;
+    bv1 = max(0, min((int)floorf(hi_v), cv)) >> 3;
+  }
+  const int wu = bu1 - bu0 + 1, wv = bv1 - bv0 + 1;
+  const bool staged = ok && wu >= 1 && wv >= 1 && wu * wv <= SLOTS;
+  win[0] = staged ? bu0 : -1;
+  win[1] = bv0;
+  win[2] = wu;
+  win[3] = wv;
+  const unsigned bytes = staged ? (unsigned)(wu * wv) * (unsigned)(sizeof(float) * kBrickFloats) : 0u;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  if (!staged) return;
+  for (int j = 0; j < wv; ++j)
+    for (int i = 0; i < wu; ++i) {
+      int b[3];
+      b[ax] = L;
+      b[u] = bu0 + i;
+      b[v] = bv0 + j;
+      const int64_t lin = ((int64_t)b[2] * dm.nbrick[1] + b[1]) * dm.nbrick[0] + b[0];
+      const float *src = dm.bricks + lin * kBrickFloats;
+      float *dst = buf + (j * wu + i) * kBrickFloats;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_addr(dst)),
+          "l"(src), "r"((unsigned)(sizeof(float) * kBrickFloats)), "r"(smem_addr(bar))
+          : "memory");
+    }
+}
+
+template <int PW, int SLOTS, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+layer_kernel(const DomainDev *__restrict__ g_domains, const __grid_constant__ ViewDev view,
+             const __grid_constant__ MarchParams mp, const float4 *__restrict__ g_lut,
+             float4 *__restrict__ rgba, float *__restrict__ depth, unsigned long long *__restrict__ samples,
+             const int *__restrict__ order, const StageOrder dorder, unsigned long long *__restrict__ stage_fail)
+{
+  constexpr int PH = 32 / PW;
+  constexpr int PX = kTile / PW;
+  const int tiles_x = (mp.width + kTile - 1) / kTile;
+  const int tile = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
+  const int tile_x = tile % tiles_x, tile_y = tile / tiles_x;
+  extern __shared__ float4 smem[];
+  float4 *lut = smem;
+  DomainDev *doms = reinterpret_cast<DomainDev *>(smem + mp.lut_size);
+  const size_t head = ((sizeof(float4) * mp.lut_size + sizeof(DomainDev) * mp.n_domains) + 127) & ~(size_t)127;
+  float *bufs = reinterpret_cast<float *>(reinterpret_cast<char *>(smem) + head);
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ int s_win[2][4];
+  __shared__ float s_cA[4][3], s_cB[4][3];
+  __shared__ int s_ax, s_lmin, s_lmax;
+
+  for (int i = threadIdx.x; i < mp.lut_size; i += kThreads) lut[i] = g_lut[i];
+  {
+    const int words = mp.n_domains * (int)(sizeof(DomainDev) / 4);
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(g_domains);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(doms);
+    for (int i = threadIdx.x; i < words; i += kThreads) dst[i] = src[i];
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&s_bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int px = tile_x * kTile + (warp % PX) * PW + (lane % PW);
+  const int py = tile_y * kTile + (warp / PX) * PH + (lane / PW);
+  const bool valid = px < mp.width && py < mp.height;
+
+  // every domain a uniform vertex field in 8^3-cell bricks with nothing to
+  // jump (the same for all threads): else the per-ray march
+  bool covered_all = true;
+  for (int d = 0; d < mp.n_domains; ++d) {
+    const DomainDev &dm = doms[d];
+    covered_all = covered_all && dm.kind == GVR_DOMAIN_UNIFORM && dm.assoc == GVR_ASSOC_VERTEX &&
+                  dm.bshift == 3 && !(mp.skip_empty && *dm.any_empty);
+  }
+  if (!covered_all) {
+    // the buffers are not used on this path: render_ray's per-ray state
+    // lives there
+    static_assert(2 * SLOTS * kBrickFloats >= kStateSlots * kThreads, "state fits the buffers");
+    float *s_state = bufs;
+    int count = 0;
+    if (valid) {
+      const uint64_t all = mp.n_domains >= 64 ? ~0ull : ((1ull << mp.n_domains) - 1ull);
+      float4 out;
+      float dep;
+      count = render_ray<1, false>(doms, all, view, mp, lut, px, py, out, dep, s_state);
+      const int64_t pix = (int64_t)py * mp.width + px;
+      rgba[pix] = out;
+      depth[pix] = dep;
+    }
+    if (samples) {
+      unsigned long long c = (unsigned long long)count;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if (lane == 0 && c) atomicAdd(samples, c);
+    }
+    return;
+  }
+
+  const Ray r = pixel_ray(view, mp, valid ? px : 0, valid ? py : 0);
+  const float t_max = valid ? canvas_ray_end(view, mp, px, py) : FLT_MAX;
+  const float dt = mp.sample_dist;
+  const float nm1 = (float)(mp.lut_size - 1);
+  float crgb[3] = {0.f, 0.f, 0.f}, ca = 0.f, cdepth = 0.f, covered = -FLT_MAX;
+  bool have = false;
+  int count = 0;
+  unsigned ph0 = 0, ph1 = 0;   // barrier phases (CTA-uniform)
+  bool staging = true;         // CTA-uniform: off after a wait gave up
+
+  for (int oi = 0; oi < dorder.n; ++oi) {
+    const DomainDev &dm = doms[dorder.d[oi]];
+    float bt0 = 0.f, bt1 = 0.f;
+    bool act = false;
+    if (valid && ca < mp.early_term) {
+      float t0, t1;
+      if (slab(dm, r, t0, t1)) {
+        bt0 = fmaxf(t0, covered);
+        bt1 = fminf(t1, t_max);
+        covered = fmaxf(covered, bt1);
+        act = true;
+      }
+    }
+    if (threadIdx.x == 0) {
+      s_lmin = INT_MAX;
+      s_lmax = -1;
+      // the tile's corner rays in this domain's grid space, and the axis
+      // its centre ray advances fastest on
+      const int x0 = tile_x * kTile, y0 = tile_y * kTile;
+      const int cx[4] = {x0, x0 + kTile - 1, x0, x0 + kTile - 1};
+      const int cy[4] = {y0, y0, y0 + kTile - 1, y0 + kTile - 1};
+      for (int c = 0; c < 4; ++c) {
+        const Ray rc = pixel_ray(view, mp, cx[c], cy[c]);
+        for (int a = 0; a < 3; ++a) {
+          s_cA[c][a] = (rc.o[a] - dm.origin[a]) * dm.inv_spacing[a];
+          s_cB[c][a] = rc.d[a] * dm.inv_spacing[a];
+        }
+      }
+      const Ray rm = pixel_ray(view, mp, x0 + kTile / 2, y0 + kTile / 2);
+      float best = -1.f;
+      int ax = 2;
+      for (int a = 0; a < 3; ++a) {
+        const float m = fabsf(rm.d[a] * dm.inv_spacing[a]);
+        if (m > best) { best = m; ax = a; }
+      }
+      s_ax = ax;
+    }
+    __syncthreads();
+    if (!__syncthreads_or(act)) continue;
+    const int ax = s_ax;
+    const float thr = mp.early_term < 1.f ? (mp.early_term - ca) / (1.f - ca) : 2.f;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float A[3], B[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      A[a] = (r.o[a] - dm.origin[a]) * dm.inv_spacing[a];
+      B[a] = r.d[a] * dm.inv_spacing[a];
+    }
+    const int cmax[3] = {dm.dims[0] - 2, dm.dims[1] - 2, dm.dims[2] - 2};
+    const int nbx = dm.nbrick[0], nby = dm.nbrick[1];
+    // this ray's layers: those of its first sample and of its interval's end
+    if (act) {
+      const float aa = ax == 0 ? A[0] : (ax == 1 ? A[1] : A[2]);
+      const float ba = ax == 0 ? B[0] : (ax == 1 ? B[1] : B[2]);
+      const int ca_max = ax == 0 ? cmax[0] : (ax == 1 ? cmax[1] : cmax[2]);
+      const int c0 = max(0, min((int)fmaf(bt0, ba, aa), ca_max)) >> 3;
+      const int c1 = max(0, min((int)fmaf(bt1, ba, aa), ca_max)) >> 3;
+      atomicMin(&s_lmin, min(c0, c1));
+      atomicMax(&s_lmax, max(c0, c1));
+    }
+    __syncthreads();
+    const bool up = s_cB[0][ax] + s_cB[1][ax] + s_cB[2][ax] + s_cB[3][ax] > 0.f;
+    const int lmin = s_lmin, lmax = s_lmax;
+    const int n_layers = lmax - lmin + 1;
+    const int Lb = up ? lmin : lmax, step = up ? 1 : -1;
+    // a ray that does not advance along the axis the tile's corner rays do
+    // (none in practice: the axis is its centre ray's dominant one) takes
+    // all its samples in the first layer, from global memory outside the
+    // window
+    const float bax = ax == 0 ? B[0] : (ax == 1 ? B[1] : B[2]);
+    const bool ordered = up ? bax > 0.f : bax < 0.f;
+    if (threadIdx.x == 0 && staging) {
+      layer_issue<SLOTS>(dm, s_cA, s_cB, ax, Lb, bufs, &s_bar[0], s_win[0]);
+      if (n_layers > 1) layer_issue<SLOTS>(dm, s_cA, s_cB, ax, Lb + step, bufs + SLOTS * kBrickFloats,
+                                           &s_bar[1], s_win[1]);
+    }
+    bool pend0 = staging, pend1 = staging && n_layers > 1;   // copies issued, not yet waited for
+    int k = 0;
+    bool live = act;
+    int last_off = -1;
+    float lc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int li = 0; li < n_layers; ++li) {
+      const int L = Lb + step * li;
+      const int b = li & 1;
+      bool use = false;
+      if (b == 0 ? pend0 : pend1) {
+        uint64_t *bar = &s_bar[b];
+        const unsigned ph = b == 0 ? ph0 : ph1;
+        bool ok = __syncthreads_and(stage_wait(bar, ph, kLayerPolls));
+        if (!ok) {
+          // the copies may still land: wait once more, longer, then read
+          // global memory for the rest of the tile
+          if (threadIdx.x == 0) atomicAdd(stage_fail, 1ull);
+          __syncthreads_and(stage_wait(bar, ph, 8 * kLayerPolls));
+          staging = false;
+        }
+        if (b == 0) { ph0 ^= 1u; pend0 = false; } else { ph1 ^= 1u; pend1 = false; }
+        use = ok && s_win[b][0] >= 0;
+      }
+      const float *buf = bufs + b * SLOTS * kBrickFloats;
+      const int wu0 = s_win[b][0], wv0 = s_win[b][1], wu = s_win[b][2], wv = s_win[b][3];
+      const int u = ax == 0 ? 1 : 0, v = ax == 2 ? 1 : 2;
+      while (live) {
+        const float t = fmaf((float)k, dt, bt0);
+        if (!(t < bt1)) { live = false; break; }
+        int c[3];
+        float w[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float g = fmaf(t, B[a], A[a]);
+          c[a] = max(0, min((int)g, cmax[a]));
+          w[a] = g - (float)c[a];
+        }
+        // (selects, not c[ax]: a runtime index would put c in local memory)
+        const int lay = (ax == 0 ? c[0] : (ax == 1 ? c[1] : c[2])) >> 3;
+        if (ordered && (up ? lay > L : lay < L)) break;   // a later layer's sample
+        ++k;
+        ++count;
+        const int loff = ((c[2] & 7) * kBrickNodes + (c[1] & 7)) * kBrickNodes + (c[0] & 7);
+        const int64_t gi = ((int64_t)(c[2] >> 3) * nby + (c[1] >> 3)) * nbx + (c[0] >> 3);
+        const int off = (int)(gi * kBrickFloats) + loff;
+        if (off != last_off) {
+          const int cu = u == 0 ? c[0] : c[1], cv = v == 1 ? c[1] : c[2];
+          const unsigned iu = (unsigned)((cu >> 3) - wu0), iv = (unsigned)((cv >> 3) - wv0);
+          if (use && iu < (unsigned)wu && iv < (unsigned)wv) {
+            const float *q = buf + (iv * wu + iu) * kBrickFloats + loff;
+            lc[0] = q[0];
+            lc[1] = q[1];
+            lc[2] = q[kBrickNodes];
+            lc[3] = q[kBrickNodes + 1];
+            lc[4] = q[kBrickNodes * kBrickNodes];
+            lc[5] = q[kBrickNodes * kBrickNodes + 1];
+            lc[6] = q[kBrickNodes * kBrickNodes + kBrickNodes];
+            lc[7] = q[kBrickNodes * kBrickNodes + kBrickNodes + 1];
+          } else {
+            const float *q = dm.bricks + off;
+            lc[0] = __ldg(q);
+            lc[1] = __ldg(q + 1);
+            lc[2] = __ldg(q + kBrickNodes);
+            lc[3] = __ldg(q + kBrickNodes + 1);
+            lc[4] = __ldg(q + kBrickNodes * kBrickNodes);
+            lc[5] = __ldg(q + kBrickNodes * kBrickNodes + 1);
+            lc[6] = __ldg(q + kBrickNodes * kBrickNodes + kBrickNodes);
+            lc[7] = __ldg(q + kBrickNodes * kBrickNodes + kBrickNodes + 1);
+          }
+          last_off = off;
+        }
+        const float c00 = lerpf(lc[0], lc[1], w[0]);
+        const float c10 = lerpf(lc[2], lc[3], w[0]);
+        const float c01 = lerpf(lc[4], lc[5], w[0]);
+        const float c11 = lerpf(lc[6], lc[7], w[0]);
+        const float val = lerpf(lerpf(c00, c10, w[1]), lerpf(c01, c11, w[1]), w[2]);
+        const float sc = __saturatef((val - mp.scalar_min) * mp.inv_range);
+        float4 col;
+        if (mp.lut_filter == GVR_LUT_LINEAR) {
+          col = lut_fetch(lut, mp.lut_size, GVR_LUT_LINEAR, sc);
+        } else {
+          col = lut_nearest(lut, nm1, sc);
+        }
+        const float wa = (1.f - acc.w) * col.w;
+        acc.x = fmaf(wa, col.x, acc.x);
+        acc.y = fmaf(wa, col.y, acc.y);
+        acc.z = fmaf(wa, col.z, acc.z);
+        acc.w += wa;
+        if (acc.w >= thr) { live = false; break; }
+      }
+      // the buffer is free again: the layer two ahead goes into it, unless
+      // no ray is left (then only the copies already issued are waited for)
+      const bool any = __syncthreads_or(live);
+      if (any && staging && li + 2 < n_layers) {
+        if (threadIdx.x == 0)
+          layer_issue<SLOTS>(dm, s_cA, s_cB, ax, L + 2 * step, bufs + b * SLOTS * kBrickFloats, &s_bar[b],
+                             s_win[b]);
+        if (b == 0) pend0 = true; else pend1 = true;
+      }
+      if (!any) break;
+    }
+    // drain copies still in flight before the buffers are reused
+    for (int b = 0; b < 2; ++b) {
+      if (!(b == 0 ? pend0 : pend1)) continue;
+      const unsigned ph = b == 0 ? ph0 : ph1;
+      if (!__syncthreads_and(stage_wait(&s_bar[b], ph, 8 * kLayerPolls))) {
+        if (threadIdx.x == 0) atomicAdd(stage_fail, 1ull);
+        staging = false;
+      }
+      if (b == 0) { ph0 ^= 1u; pend0 = false; } else { ph1 ^= 1u; pend1 = false; }
+    }
+    __syncthreads();
+    // the domain's partial, as render_ray blends it
+    if (act && !(acc.w < mp.alpha_cull)) {
+      if (!have) {
+        crgb[0] = acc.x; crgb[1] = acc.y; crgb[2] = acc.z; ca = acc.w;
+        cdepth = bt1;
+        have = true;
+      } else if (ca < 1.f && acc.w != 0.f) {
+        const float op = 1.f - ca;
+        crgb[0] = fmaf(op, acc.x, crgb[0]);
+        crgb[1] = fmaf(op, acc.y, crgb[1]);
+        crgb[2] = fmaf(op, acc.z, crgb[2]);
+        ca = fminf(fmaf(op, acc.w, ca), 1.f);
+      }
+    }
+  }
+  if (valid) {
+    float4 out;
+    float dep;
+    finish_pixel(view, mp, px, py, have, crgb, ca, cdepth, out, dep);
+    const int64_t pix = (int64_t)py * mp.width + px;
+    rgba[pix] = out;
+    depth[pix] = dep;
+  }
+  if (samples) {
+    unsigned long long cnt = (unsigned long long)count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0 && cnt) atomicAdd(samples, cnt);
+  }
+}
+
 // Many views in one persistent launch. A device counter hands out work items
 // of `tiles_per_item` consecutive 16x16 tiles; items run through every tile
 // of view 0, then view 1, ... so neighbouring CTAs share bricks in L2. Each
@@ -1601,6 +1976,26 @@ cudaError_t launch_staged(const DomainDev *d_domains, const ViewDev &view, const
                           const StageOrder &order, unsigned long long *d_stage_fail,
                           cudaStream_t stream)
 {
+  if (tuning.staged == 2) {
+    // the layer walk, two buffers: 9 bricks per window (3 x 3) at 3 CTAs per
+    // SM, or 12 at 2 (min_blocks 4)
+    const bool wide = tuning.min_blocks >= 4;
+    const int slots = wide ? 12 : 9;
+    StagedFn lfn = wide ? (tuning.packet_w == 4 ? layer_kernel<4, 12, 2> : layer_kernel<8, 12, 2>)
+                        : (tuning.packet_w == 4 ? layer_kernel<4, 9, 3> : layer_kernel<8, 9, 3>);
+    auto lsmem = [slots](int lut_size, int n_domains) {
+      const size_t head = (sizeof(float4) * lut_size + sizeof(DomainDev) * n_domains + 127) & ~(size_t)127;
+      return head + 2 * sizeof(float) * kBrickFloats * slots;
+    };
+    cudaError_t e = cudaFuncSetAttribute(lfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)lsmem(kMaxLut, kMaxDomains));
+    if (e != cudaSuccess) return e;
+    const int64_t tiles = (int64_t)((mp.width + kTile - 1) / kTile) * ((mp.height + kTile - 1) / kTile);
+    lfn<<<(unsigned)tiles, kThreads, lsmem(mp.lut_size, mp.n_domains), stream>>>(
+        d_domains, view, mp, d_lut, d_rgba, d_depth, d_samples, d_order, order, d_stage_fail);
+    count_launch();
+    return cudaGetLastError();
+  }
   StagedFn fn = select_staged(tuning);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)staged_smem(kMaxLut, kMaxDomains));

@@ -31,7 +31,8 @@ CANDIDATES = ([dict(packet_w=p, unroll=u, min_blocks=m)
                for p, u, m in itertools.product((8, 4), (3, 4), (3, 4)) if (u, m) != (3, 4)])
 # shared-memory brick staging (plain path, uniform vertex scenes; elsewhere
 # the scene runs the gather kernel of the same packet shape)
-STAGED_CANDIDATES = [dict(packet_w=p, unroll=1, min_blocks=3, staged=1) for p in (8, 4, 16)]
+STAGED_CANDIDATES = ([dict(packet_w=p, unroll=1, min_blocks=3, staged=1) for p in (8, 4, 16)] +
+                     [dict(packet_w=p, unroll=1, min_blocks=m, staged=2) for p in (8, 4) for m in (3, 4)])
 # the batch kernel has no 3- or 4-sample variant (it would run as 2) and no staging
 BATCH_CANDIDATES = [c for c in CANDIDATES if c["unroll"] <= 2]
 CACHE = Path(os.environ.get("GVR_TUNE_CACHE", Path.home() / ".cache" / "gvr_tune.json"))
@@ -123,7 +124,8 @@ def autotune(scene, camera, params, reps: int = 3, use_cache: bool = True, stage
     cands = STAGED_CANDIDATES if only_staged else CANDIDATES + (STAGED_CANDIDATES if staged else [])
     for cand in cands:
         scene.set_tuning(**cand)
-        name = f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}" + ("s" if cand.get("staged") else "")
+        name = (f"p{cand['packet_w']}u{cand['unroll']}m{cand['min_blocks']}"
+                + {0: "", 1: "s", 2: "L"}[cand.get("staged", 0)])
         results[name] = (_time(scene, camera, params, rgba, depth, stream, reps), cand)
     name, (ms, best) = min(results.items(), key=lambda kv: kv[1][0])
     # the winner again with each tile order, timed back to back
