@@ -167,7 +167,8 @@ class Scene:
     def set_tuning(self, packet_w: int = 8, unroll: int = 2, min_blocks: int = 4, staged: int = 0,
                    tile_order: int = 0) -> None:
         """Launch shape of the march kernel, whether the plain path stages
-        bricks in shared memory and how it orders its tiles (0 centre
+        bricks in shared memory (0 no, 1 per slab of ray distance, 2 per
+        brick layer, double-buffered) and how it orders its tiles (0 centre
         first, 1 longest first for each view); images depend on none."""
         N.call("gvr_scene_set_tuning", self.handle, int(packet_w), int(unroll), int(min_blocks))
         N.call("gvr_scene_set_staging", self.handle, int(staged))

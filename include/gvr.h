@@ -297,9 +297,13 @@ GVR_API int gvr_scene_set_brick_cells(gvr_scene *scene, int cells);
 /* How the plain march reads bricks: mode 0 gathers each sample's corners
  * through the L1 cache; mode 1 stages, per 16 x 16 tile and slab of ray
  * distance, the bricks the tile's rays cross into shared memory with bulk
- * async copies and reads them there (scenes of uniform vertex-field domains
- * in 8^3-cell bricks only; other scenes, and the batch path, use mode 0). Images are the same
- * either way. Set by the autotuner (ascent_gb300.tune); the march the
+ * async copies and reads them there; mode 2 walks each domain's brick
+ * layers along the rays' dominant axis, bulk-copying each layer's window of
+ * bricks into one of two shared-memory buffers while the rays sample the
+ * other (modes 1 and 2: scenes of uniform vertex-field domains in 8^3-cell
+ * bricks only; other scenes, and the batch path, use mode 0; mode 2 also
+ * leaves scenes with empty bricks to jump to the gather). Images are the
+ * same in every mode. Set by the autotuner (ascent_gb300.tune); the march the
  * reference runs is VTK-m's (VolumeRenderer.cpp:258, 523-528), so no
  * counterpart. */
 GVR_API int gvr_scene_set_staging(gvr_scene *scene, int mode);
