@@ -5,7 +5,8 @@ shared-memory staged march's exactly (an independent implementation of the
 same per-domain order, sample positions and blend) and stay within the
 parity bar of the FP64 oracle, at the 16-domain limit and past it (18
 domains take the per-domain loop), for a camera outside and inside the
-volume, and with an opaque canvas that ends rays part-way.
+volume, with an opaque canvas that ends rays part-way, and in the batch
+kernel.
 """
 import numpy as np
 import pytest
@@ -75,3 +76,28 @@ def test_domain_walk_over_a_canvas():
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
     assert out[0][2] == out[1][2]
+
+
+def test_domain_walk_in_the_batch_kernel():
+    """The batch kernel takes the one-loop walk for tiles whose domain mask
+    has two or more domains: its views equal the per-view renders and the
+    oracle's."""
+    wl = W.plain_small(n=57, width=72, height=64, parts=(2, 2, 2))
+    cams = S.cinema_cameras(wl.bounds, W.cinema_angles(2, 2))
+    p = V.workload_params(wl)
+    with S.Scene(0) as sc:
+        V.load_workload(sc, wl)
+        rgba, depth, n = sc.render_batch(cams, p, count_samples=True)
+        total = 0
+        for v, cam in enumerate(cams):
+            g, gd, gn = sc.render(cam, p, count_samples=True)
+            np.testing.assert_array_equal(rgba[v], g)
+            np.testing.assert_array_equal(depth[v], gd)
+            total += gn
+        assert n == total
+    ocams = O.cinema_cameras(wl.bounds, W.cinema_angles(2, 2))
+    osc = oracle_scene(wl)
+    op = O.workload_params(wl)
+    for v in range(len(cams)):
+        o, _, _ = osc.render(ocams[v], op)
+        assert_parity(rgba[v], o)
